@@ -1,0 +1,218 @@
+/*
+ * soundersim_gb300.h -- C ABI of the GB300 (sm_103a) coherent facet kernels.
+ *
+ * Plain C: device pointers, sizes, status codes; no exceptions and no
+ * framework types cross this boundary. Every pointer marked (device) must
+ * be a CUDA device pointer owned by the caller; nothing here retains a
+ * pointer after the call returns. Work is enqueued on `stream` (a
+ * cudaStream_t passed as void*, NULL = legacy default stream) and the
+ * functions return without synchronising, except where noted.
+ *
+ * The reference (soundersim, paths relative to src/soundersim/) exposes this
+ * path as two Python functions, kernels/coherent.py:247-362
+ * (coherent_cluttergram) and kernels/multilayer.py:594-770
+ * (refracted_cluttergram). Their host preparation (along-track sort, block
+ * windows, lookup tables) stays on the host in the Python mirror
+ * (radar_sounder_simulator_gb300.kernels); the jitted device programs they
+ * launch (coherent.py:172-244 `_coherent_fn`, multilayer.py:333-591
+ * `_refracted_fn`) are what the entry points below replace.
+ */
+#ifndef SOUNDERSIM_GB300_H
+#define SOUNDERSIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ----------------------------------------------------- */
+#define SS_OK 0
+#define SS_ERR_ARG 1         /* invalid argument (null pointer, bad size)  */
+#define SS_ERR_CUDA 2        /* a CUDA runtime call failed                  */
+#define SS_ERR_UNSUPPORTED 3 /* option combination not implemented          */
+#define SS_ERR_SCRATCH 4     /* scratch buffer smaller than required        */
+
+/* ---- enumerations ------------------------------------------------------ */
+#define SS_PREC_FP64 0   /* plain float64 form (the drop-in)               */
+#define SS_PREC_SPLIT 1  /* float32 bulk, double-float range/phase/bins    */
+
+/* antenna.py:204-258 gain_fn kinds */
+#define SS_PAT_ISOTROPIC 0
+#define SS_PAT_DIPOLE 1
+#define SS_PAT_ARRAY 2
+#define SS_PAT_ARRAY_TAPERED 3
+#define SS_PAT_FINITE_DIPOLE 4
+#define SS_PAT_TABULATED 5
+
+/* roughness.py:217-276 d_phi variants */
+#define SS_ROUGH_NONE 0
+#define SS_ROUGH_GAUSS_FULL 1  /* Eqs 22-24 through the Faddeeva function  */
+#define SS_ROUGH_GAUSS_AREA 2  /* area-only, Gaussian ACF                  */
+#define SS_ROUGH_EXP_AREA 3    /* area-only, exponential ACF               */
+
+/* ---- inputs ------------------------------------------------------------ */
+
+/* Target facets in along-track sorted order, structure of arrays, float32
+ * (the reference quantises facet geometry to float32: coherent.py:298-301,
+ * multilayer.py:699-702). Optional arrays may be NULL. */
+typedef struct {
+  const float *cx, *cy, *cz;       /* (device) centroid                     */
+  const float *nx, *ny, *nz;       /* (device) unit normal                  */
+  const float *e1x, *e1y, *e1z;    /* (device) mean edge along +column      */
+  const float *e2x, *e2y, *e2z;    /* (device) mean edge along +row         */
+  const float *area;               /* (device) |e1 x e2|                    */
+  const float *gamma_f32;          /* (device) per-facet field gamma or NULL
+                                      (surface path, float32 like
+                                      coherent.py:338-345)                  */
+  const double *gamma_f64;         /* (device) per-facet field gamma or NULL
+                                      (refracted path, float64 like
+                                      multilayer.py:728-735)                */
+  const float *sigma;              /* (device) per-facet rms height or NULL */
+  const float *corr;               /* (device) per-facet corr length or NULL*/
+  const float *phasor;             /* (device) complex64 speckle phasors
+                                      interleaved (re, im), or NULL        */
+  const double *diffuse_amp;       /* (device) diffuse field amp or NULL    */
+  const float *diffuse_phasor;     /* (device) complex64 diffuse phasors    */
+  int32_t n_facets;
+} ss_facets;
+
+/* Per-trace inputs. */
+typedef struct {
+  const double *pos;  /* (device) (T, 3) platform positions, local frame    */
+  const double *uct;  /* (device) (T, 3) cross-track unit vectors; used with
+                         split_sides only (else may be NULL)                 */
+  const double *pv;   /* (device) (T, pv_len) antenna pattern vectors, or
+                         NULL when isotropic                                 */
+  const int32_t *off; /* (device) (T,) first facet block of each trace's
+                         along-track window (geometry.py:63-78)              */
+  int32_t n_traces;
+  int32_t pv_len;     /* 3, or 6 for the array kinds ((2,3) frame)          */
+} ss_traces;
+
+/* Antenna pattern (antenna.py:76-118 pattern_args). pa/pb are device
+ * arrays: array -> pa[0] = n_elements, pb[0..3]; array_tapered -> pa (2, n)
+ * tx/rx weights, pb[0..3]; finite_dipole -> pa[0] = length_lam; tabulated
+ * -> pa theta samples (rad, ascending), pb gains (n each). */
+typedef struct {
+  int32_t kind;
+  int32_t n;          /* array_tapered: elements; tabulated: samples        */
+  const double *pa;   /* (device) or NULL                                    */
+  const double *pb;   /* (device) or NULL                                    */
+} ss_pattern;
+
+/* Sub-facet roughness of the target interface (roughness.py). */
+typedef struct {
+  int32_t kind;       /* SS_ROUGH_*                                          */
+  int32_t n_terms;    /* static series length (roughness.py:189-196)         */
+  double sigma;       /* scalar rms height (used when facets.sigma == NULL)  */
+  double corr;        /* scalar corr length (used when facets.corr == NULL)  */
+} ss_roughness;
+
+/* Surface coherent kernel options (coherent.py:247-362 keywords). */
+typedef struct {
+  double k;           /* wavenumber (rad/m)                                  */
+  double gamma;       /* scalar field reflection coefficient                 */
+  double t0, dt, c;   /* fast-time window start, bin width, speed of light  */
+  double taper_s;     /* off-specular taper s_eff (used when taper != 0)     */
+  int32_t n_samples;
+  int32_t block_size; /* culling block size (facets)                         */
+  int32_t n_win;      /* blocks per trace window                             */
+  int32_t split_sides;
+  int32_t interp_bins;
+  int32_t taper;
+  int32_t precision;  /* SS_PREC_*                                           */
+} ss_coherent_opts;
+
+/* Outputs. Exactly one of field_c128 / field_c64 is non-NULL. Layout
+ * (T, n_samples) or, with split_sides, (T, n_samples, 2) [left, right]
+ * (coherent.py:360-361). */
+typedef struct {
+  double *field_c128;  /* (device) complex128 interleaved, or NULL          */
+  float *field_c64;    /* (device) complex64 interleaved, or NULL           */
+  double *dropped;     /* (device) (T,) out-of-window power                 */
+} ss_output;
+
+/* ---- surface coherent facet sum ------------------------------------- */
+
+/* Bytes of device scratch that ss_coherent_fwd needs for these shapes
+ * (per-CTA partial histograms, reduced deterministically afterwards).
+ * Replaces nothing in the reference (XLA allocates internally). */
+size_t ss_coherent_scratch_bytes(const ss_coherent_opts *opts,
+                                 int32_t n_traces, int32_t n_facets);
+
+/* Binned coherent field of every trace over the culled target facets.
+ * Replaces the jitted vmap(one_trace) program of
+ * kernels/coherent.py:172-244 (`_coherent_fn`), called at
+ * kernels/coherent.py:350-358; the returned field already carries the
+ * absolute carrier phase (the reference's phase_ref fold-back at
+ * coherent.py:359 is folded in). `scratch` (device) must hold
+ * ss_coherent_scratch_bytes(...) bytes. */
+int ss_coherent_fwd(const ss_coherent_opts *opts, const ss_facets *facets,
+                    const ss_traces *traces, const ss_pattern *pattern,
+                    const ss_roughness *rough, const ss_output *out,
+                    void *scratch, size_t scratch_bytes, void *stream);
+
+/* ---- refracted multilayer facet sum ---------------------------------- */
+
+#define SS_MAX_IFACE 8  /* crossed interfaces per call (after padding) */
+
+/* One crossed interface: its facet lookup table and mean plane
+ * (multilayer.py:269-283 `_grid_consts`; joint no-op pads per :286-330 are
+ * 1x1 tables with a zero affine fit). */
+typedef struct {
+  const float *table;     /* (device) (ny, nx, 6) float32 [centre, normal]  */
+  int32_t ny, nx;
+  double coef[6];         /* (3, 2) row-major fit (x, y, 1) -> (row, col)  */
+  double mean_point[3];   /* area-weighted mean point                       */
+  double mean_normal[3];  /* unit area-weighted mean normal                 */
+} ss_interface;
+
+/* Refracted kernel options (multilayer.py:594-770 keywords). The small
+ * per-leg arrays are HOST pointers, copied at the call. */
+typedef struct {
+  int32_t n_crossed;             /* crossed interfaces incl. joint pads     */
+  int32_t k_pad;                 /* leading no-op pads (joint only)         */
+  const ss_interface *crossed;   /* (host) n_crossed descriptors, top-down  */
+  const double *n_leg;           /* (host) n_crossed + 1 refractive indices */
+  const double *eps_leg;         /* (host) n_crossed + 1 permittivities     */
+  const double *att_leg;         /* (host) n_crossed + 1 one-way dB/km      */
+  const double *sigma_crossed;   /* (host) n_crossed rms heights, or NULL   */
+  double k0, gamma, t0, dt, c;
+  double taper_s;                /* used when taper != 0                    */
+  double diffuse_exp;            /* cos^n law of the diffuse channel        */
+  int32_t n_samples, block_size, n_win;
+  int32_t split_sides;
+  int32_t coherent;              /* 1 coherent field, 0 incoherent power    */
+  int32_t joint;                 /* 0 sequential chain, 1 joint solve       */
+  int32_t joint_newton, joint_backtrack;
+  int32_t taper;
+  int32_t precision;             /* SS_PREC_*                               */
+} ss_refracted_opts;
+
+/* Scratch bytes ss_refracted_fwd needs for these shapes. */
+size_t ss_refracted_scratch_bytes(const ss_refracted_opts *opts,
+                                  int32_t n_traces, int32_t n_facets);
+
+/* Binned refracted-path contributions of one target interface under the
+ * crossed stack. Replaces the jitted vmap(one_trace) program of
+ * kernels/multilayer.py:333-591 (`_refracted_fn`: `path` :352-406,
+ * `path_joint` :408-457, `step` :464-583), called at
+ * kernels/multilayer.py:758-767. Coherent mode writes the complex field,
+ * incoherent mode the power in the real part (imaginary part zero). */
+int ss_refracted_fwd(const ss_refracted_opts *opts, const ss_facets *target,
+                     const ss_traces *traces, const ss_pattern *pattern,
+                     const ss_roughness *rough, const ss_output *out,
+                     void *scratch, size_t scratch_bytes, void *stream);
+
+/* Library build string (kernel version, arch) for result provenance. */
+const char *ss_version(void);
+
+/* Last CUDA error string seen by the library (thread-local), or "". */
+const char *ss_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SOUNDERSIM_GB300_H */

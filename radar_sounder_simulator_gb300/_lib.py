@@ -1,0 +1,106 @@
+"""ctypes binding of ``libsoundercuda.so`` (the C ABI in
+``include/soundersim_gb300.h``).
+
+The library is built in-tree (``radar_sounder_simulator_gb300.build``). There
+is no fallback: if it cannot be loaded, every entry point raises.
+"""
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsoundercuda.so")
+
+SS_OK, SS_ERR_ARG, SS_ERR_CUDA, SS_ERR_UNSUPPORTED, SS_ERR_SCRATCH = range(5)
+PREC = {"fp64": 0, "split": 1}
+PATTERN = {"isotropic": 0, "dipole": 1, "array": 2, "array_tapered": 3,
+           "finite_dipole": 4, "tabulated": 5}
+ROUGH_NONE, ROUGH_GAUSS_FULL, ROUGH_GAUSS_AREA, ROUGH_EXP_AREA = range(4)
+
+_f = C.POINTER(C.c_float)
+_d = C.POINTER(C.c_double)
+_i = C.POINTER(C.c_int32)
+
+
+class Facets(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in (
+        "cx", "cy", "cz", "nx", "ny", "nz", "e1x", "e1y", "e1z", "e2x",
+        "e2y", "e2z", "area", "gamma_f32", "gamma_f64", "sigma", "corr",
+        "phasor", "diffuse_amp", "diffuse_phasor")] + [("n_facets", C.c_int32)]
+
+
+class Traces(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("uct", C.c_void_p), ("pv", C.c_void_p),
+                ("off", C.c_void_p), ("n_traces", C.c_int32),
+                ("pv_len", C.c_int32)]
+
+
+class Pattern(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("n", C.c_int32), ("pa", C.c_void_p),
+                ("pb", C.c_void_p)]
+
+
+class Roughness(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("n_terms", C.c_int32),
+                ("sigma", C.c_double), ("corr", C.c_double)]
+
+
+class CoherentOpts(C.Structure):
+    _fields_ = [("k", C.c_double), ("gamma", C.c_double), ("t0", C.c_double),
+                ("dt", C.c_double), ("c", C.c_double),
+                ("taper_s", C.c_double), ("n_samples", C.c_int32),
+                ("block_size", C.c_int32), ("n_win", C.c_int32),
+                ("split_sides", C.c_int32), ("interp_bins", C.c_int32),
+                ("taper", C.c_int32), ("precision", C.c_int32)]
+
+
+class Output(C.Structure):
+    _fields_ = [("field_c128", C.c_void_p), ("field_c64", C.c_void_p),
+                ("dropped", C.c_void_p)]
+
+
+# entry point name -> (restype, argtypes); the ABI surface the tests check
+SIGNATURES = {
+    "ss_coherent_scratch_bytes": (C.c_size_t, [C.POINTER(CoherentOpts),
+                                               C.c_int32, C.c_int32]),
+    "ss_coherent_fwd": (C.c_int, [C.POINTER(CoherentOpts), C.POINTER(Facets),
+                                  C.POINTER(Traces), C.POINTER(Pattern),
+                                  C.POINTER(Roughness), C.POINTER(Output),
+                                  C.c_void_p, C.c_size_t, C.c_void_p]),
+    "ss_version": (C.c_char_p, []),
+    "ss_last_error": (C.c_char_p, []),
+}
+
+_lib = None
+
+
+class LibraryMissing(RuntimeError):
+    pass
+
+
+def lib():
+    """Load (once) and return the CUDA library; raises when it is absent."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise LibraryMissing(
+                f"{LIB_PATH} not built: run `python -m "
+                "radar_sounder_simulator_gb300.build` (there is no CPU "
+                "fallback)")
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status, what):
+    """Map a library status code to the reference's exception types."""
+    if status == SS_OK:
+        return
+    msg = lib().ss_last_error().decode(errors="replace")
+    if status in (SS_ERR_ARG, SS_ERR_UNSUPPORTED):
+        raise ValueError(f"{what}: {msg}")
+    raise RuntimeError(f"{what} failed (status {status}): {msg}")

@@ -1,0 +1,188 @@
+"""Drop-in ``coherent_cluttergram`` on GB300.
+
+Mirrors soundersim ``kernels/coherent.py:247-362``: same positional and
+keyword arguments, the same host conventions (float32 facet quantisation,
+along-track culling, ``ValueError`` texts), NumPy in and NumPy out. The
+device program is the CUDA library (``ss_coherent_fwd``); there is no CPU
+path.
+
+Extensions (keyword-only, defaults keep the reference behaviour):
+``precision`` -- "fp64" (default, the float64 form) or "split" (float32 bulk
+with double-float range, phase and bins); ``out_dtype`` -- complex64
+(reference) or complex128; ``roughness`` may carry per-facet (N,) sigma and
+correlation-length arrays in place of the scalars.
+"""
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from . import _lib
+from .geometry import cull_plan
+
+TWO_PI = 2.0 * np.pi
+
+
+def _dev(a, dtype, device):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=dtype)).to(
+        device, non_blocking=False)
+
+
+def _ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+class DeviceFacets:
+    """Target facets staged on the device in along-track order (SoA)."""
+
+    def __init__(self, soa, extras, n):
+        self.soa = soa          # (13, N) float32: c(3) n(3) e1(3) e2(3) area
+        self.extras = extras    # name -> tensor (gamma_f32, sigma, corr, ...)
+        self.n = n
+
+    def struct(self):
+        f = _lib.Facets()
+        names = ("cx", "cy", "cz", "nx", "ny", "nz", "e1x", "e1y", "e1z",
+                 "e2x", "e2y", "e2z", "area")
+        row = self.soa.stride(0) * 4
+        base = self.soa.data_ptr()
+        for j, nm in enumerate(names):
+            setattr(f, nm, base + j * row)
+        for nm, t in self.extras.items():
+            setattr(f, nm, t.data_ptr())
+        f.n_facets = self.n
+        return f
+
+
+def stage_facets(centers, normals, areas, e1, e2, order, device, *,
+                 gamma=None, sigma=None, corr=None, phasors=None):
+    """Sort, quantise to float32 and upload the facet SoA (one copy)."""
+    n = len(order)
+    soa = np.empty((13, n), np.float32)
+    soa[0:3] = np.asarray(centers, np.float32)[order].T
+    soa[3:6] = np.asarray(normals, np.float32)[order].T
+    soa[6:9] = np.asarray(e1, np.float32)[order].T
+    soa[9:12] = np.asarray(e2, np.float32)[order].T
+    soa[12] = np.asarray(areas, np.float32)[order]
+    extras = {}
+    if gamma is not None:
+        extras["gamma_f32"] = _dev(np.asarray(gamma, np.float32)[order],
+                                   np.float32, device)
+    if sigma is not None:
+        extras["sigma"] = _dev(np.asarray(sigma, np.float32)[order],
+                               np.float32, device)
+    if corr is not None:
+        extras["corr"] = _dev(np.asarray(corr, np.float32)[order],
+                              np.float32, device)
+    if phasors is not None:
+        ph = np.asarray(phasors, np.complex64)[order]
+        extras["phasor"] = _dev(ph.view(np.float32), np.float32, device)
+    return DeviceFacets(_dev(soa, np.float32, device), extras, n)
+
+
+def pattern_struct(pattern, n_traces, device):
+    """(kind, pv, pa, pb) tuple -> (Pattern struct, pv tensor, keep-alive)."""
+    if pattern is None:
+        return _lib.Pattern(0, 0, None, None), None, 0, []
+    kind, pv, pa, pb = pattern
+    if kind not in _lib.PATTERN:
+        raise ValueError(f"unknown pattern kind {kind!r}")
+    pv = np.asarray(pv, np.float64).reshape(n_traces, -1)
+    pa = np.atleast_1d(np.asarray(pa, np.float64))
+    pb = np.atleast_1d(np.asarray(pb, np.float64))
+    n = 0
+    if kind == "array_tapered":
+        n = pa.shape[-1] if pa.ndim > 1 else len(pa) // 2
+    elif kind == "tabulated":
+        n = len(pa)
+    pa_t = _dev(pa.ravel(), np.float64, device)
+    pb_t = _dev(pb.ravel(), np.float64, device)
+    pv_t = _dev(pv, np.float64, device)
+    st = _lib.Pattern(_lib.PATTERN[kind], n, pa_t.data_ptr(), pb_t.data_ptr())
+    return st, pv_t, pv.shape[1], [pa_t, pb_t]
+
+
+def rough_struct(roughness, d_phi_area):
+    """Reference roughness tuple -> (Roughness struct, per-facet arrays)."""
+    if roughness is None:
+        return _lib.Roughness(_lib.ROUGH_NONE, 0, 0.0, 0.0), None, None, None
+    sigma, lcorr, phasors, n_terms, *rest = roughness
+    acf = rest[0] if rest else "gaussian"
+    if acf == "exponential" and not d_phi_area:
+        raise ValueError("roughness acf='exponential' requires the "
+                         "area-only D_Phi (d_phi_area / grazing fix)")
+    if acf not in ("gaussian", "exponential"):
+        raise ValueError(f"unknown roughness acf {acf!r} (want one of "
+                         "('gaussian', 'exponential'))")
+    kind = (_lib.ROUGH_EXP_AREA if acf == "exponential" else
+            _lib.ROUGH_GAUSS_AREA if d_phi_area else _lib.ROUGH_GAUSS_FULL)
+    s_arr = sigma if np.ndim(sigma) else None
+    l_arr = lcorr if np.ndim(lcorr) else None
+    st = _lib.Roughness(kind, int(n_terms),
+                        0.0 if s_arr is not None else float(sigma),
+                        0.0 if l_arr is not None else float(lcorr))
+    return st, s_arr, l_arr, phasors
+
+
+def coherent_cluttergram(positions, u_ct, centers, normals, areas, e1, e2, *,
+                         k, gamma, t0, dt, n_samples, c, split_sides=False,
+                         interp_bins=False, pattern=None, roughness=None,
+                         taper_s=None, d_phi_area=False, block_size=None,
+                         window_cull=True, precision="fp64",
+                         out_dtype=np.complex64, device=None):
+    """Binned coherent field for every trace (coherent.py:247-362).
+
+    Returns ``(field, dropped)``: field (T, n_samples) or (T, n_samples, 2)
+    [left, right] with the absolute carrier phase, dropped (T,) float32
+    out-of-window power."""
+    device = torch.device(device or "cuda")
+    pos = np.asarray(positions, np.float64)
+    T = len(pos)
+    n = np.asarray(centers).shape[0]
+    plan = cull_plan(pos, centers, t0=t0, dt=dt, n_samples=n_samples, c=c,
+                     block_size=block_size, target_pairs=1 << 19,
+                     window_cull=window_cull)
+    gamma_arr = np.asarray(gamma, np.float32)
+    gamma_facet = gamma_arr.ndim > 0
+    if gamma_facet and gamma_arr.shape != (n,):
+        raise ValueError(f"per-facet gamma shape {gamma_arr.shape} != ({n},)")
+    rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
+    fac = stage_facets(centers, normals, areas, e1, e2, plan.order, device,
+                       gamma=gamma_arr if gamma_facet else None,
+                       sigma=s_arr, corr=l_arr, phasors=phasors)
+    pst, pv_t, pv_len, keep = pattern_struct(pattern, T, device)
+    pos_t = _dev(pos, np.float64, device)
+    uct_t = _dev(np.asarray(u_ct, np.float64).reshape(T, 3), np.float64,
+                 device)
+    off_t = _dev(plan.off, np.int32, device)
+    tr = _lib.Traces(pos_t.data_ptr(), uct_t.data_ptr(),
+                     pv_t.data_ptr() if pv_t is not None else None,
+                     off_t.data_ptr(), T, pv_len)
+    opts = _lib.CoherentOpts(
+        float(k), 0.0 if gamma_facet else float(gamma), float(t0), float(dt),
+        float(c), float(taper_s or 0.0), int(n_samples), plan.block_size,
+        plan.n_win, int(bool(split_sides)), int(bool(interp_bins)),
+        int(taper_s is not None), _lib.PREC[precision])
+    L = _lib.lib()
+    nbytes = L.ss_coherent_scratch_bytes(C.byref(opts), T, n)
+    if nbytes == 0:
+        raise ValueError("unsupported sizes for the coherent kernel")
+    scratch = torch.empty(nbytes, dtype=torch.uint8, device=device)
+    n_seg = n_samples * (2 if split_sides else 1)
+    field = torch.empty((T, n_seg, 2), dtype=torch.float64, device=device)
+    dropped = torch.empty(T, dtype=torch.float64, device=device)
+    out = _lib.Output(field.data_ptr(), None, dropped.data_ptr())
+    fst = fac.struct()
+    stream = torch.cuda.current_stream(device).cuda_stream
+    st = L.ss_coherent_fwd(C.byref(opts), C.byref(fst), C.byref(tr),
+                           C.byref(pst), C.byref(rst), C.byref(out),
+                           C.c_void_p(scratch.data_ptr()), nbytes,
+                           C.c_void_p(stream))
+    _lib.check(st, "ss_coherent_fwd")
+    f = field.cpu().numpy()
+    res = (f[..., 0] + 1j * f[..., 1]).astype(out_dtype)
+    if split_sides:
+        res = res.reshape(T, n_samples, 2)
+    del keep
+    return res, dropped.cpu().numpy().astype(np.float32)

@@ -1,0 +1,496 @@
+// Split-precision surface coherent kernel.
+//
+// Same decomposition as the FP64 form (ss_coherent.cu). Per pair, only three
+// quantities need more than float32:
+//   * the slant range r (20 km at 1 mm f32 ulp; 1e-3 rad at 450 MHz needs
+//     ~50 um): carried as double-float from a double-float platform position
+//     and the float32 facet centroid (exact), one rsqrt + Newton correction;
+//   * the carrier phase 2 k r: a double-float product reduced modulo 2 pi
+//     with a two-constant Cody-Waite step (exact first step by construction),
+//     then MUFU sin/cos on an argument in [-pi, pi];
+//   * the fast-time bin floor((2r/c - t0)/dt): evaluated from the
+//     double-float range; a pair whose fractional bin position lies within
+//     1e-6 of an edge is re-binned with the float64 round-to-nearest chain of
+//     the oracle, so bins are bit-identical to the float64 form.
+// Everything else (incidence, sincs, taper, antenna gain, roughness series)
+// runs in float32; histograms accumulate float32 per CTA chunk and chunks are
+// summed in float64 by the reduce kernel.
+#include "ss_coherent.cuh"
+#include "ss_df.cuh"
+
+#define SS_PAT_MAX 256
+
+namespace ss {
+
+__constant__ float kTwoPiH = 6.28318548202514648f;     // float(2 pi)
+__constant__ float kTwoPiM = -1.74845553146951e-07f;   // 2 pi - kTwoPiH
+
+__device__ __forceinline__ float reduce_2pi(float x) {
+  const float n = rintf(x * 0.159154943091895336f);
+  float r = __fmaf_rn(-n, 6.28318548202514648f, x);
+  return __fmaf_rn(-n, -1.74845553146951e-07f, r);
+}
+
+__device__ __forceinline__ float sin_red(float x) {
+  return __sinf(reduce_2pi(x));
+}
+
+__device__ __forceinline__ float cos_red(float x) {
+  return __cosf(reduce_2pi(x));
+}
+
+// sin(x)/x
+__device__ __forceinline__ float sinc32(float x) {
+  if (fabsf(x) < 1e-4f) return 1.0f - x * x * (1.0f / 6.0f);
+  return __fdividef(sin_red(x), x);
+}
+
+__device__ __forceinline__ float dot3f(float ax, float ay, float az, float bx,
+                                       float by, float bz) {
+  return __fmaf_rn(az, bz, __fmaf_rn(ay, by, ax * bx));
+}
+
+__device__ __forceinline__ float element_field32(float cb, float q,
+                                                 float enabled) {
+  if (enabled == 0.0f) return 1.0f;
+  if (!(cb >= 0.0f)) return 0.0f;
+  float c = fminf(fmaxf(cb, 0.0f), 1.0f);
+  return c > 0.0f ? __powf(c, 0.5f * q) : (q == 0.0f ? 1.0f : 0.0f);
+}
+
+// float32 twin of gain64 (antenna.py:204-258); pa then pb staged in `tab`.
+__device__ __forceinline__ float gain32(int kind, int n, int pa_len,
+                                        const float *tab, const float *pv,
+                                        float dx, float dy, float dz) {
+  const float *pa = tab, *pb = tab + pa_len;
+  switch (kind) {
+    case SS_PAT_DIPOLE: {
+      float ca = dot3f(dx, dy, dz, pv[0], pv[1], pv[2]);
+      float s = sqrtf(fmaxf(1.0f - ca * ca, 1e-12f));
+      return __fdividef(__cosf(1.57079632679f * ca), s);
+    }
+    case SS_PAT_ARRAY: {
+      float ne = pa[0];
+      float u = dot3f(dx, dy, dz, pv[0], pv[1], pv[2]);
+      float ct = dot3f(dx, dy, dz, pv[3], pv[4], pv[5]);
+      float x = 3.14159265359f * pb[0] * u;
+      float sx = sin_red(x);
+      float af = fabsf(sx) < 1e-5f ? __fdividef(cos_red(ne * x), cos_red(x))
+                                   : __fdividef(sin_red(ne * x), ne * sx);
+      return pb[1] * element_field32(ct, pb[2], pb[3]) * fabsf(af);
+    }
+    case SS_PAT_ARRAY_TAPERED: {
+      float u = dot3f(dx, dy, dz, pv[0], pv[1], pv[2]);
+      float ct = dot3f(dx, dy, dz, pv[3], pv[4], pv[5]);
+      float ctx = 0, stx = 0, crx = 0, srx = 0, wt = 0, wr = 0;
+      for (int j = 0; j < n; ++j) {
+        float mj = (float)j - 0.5f * (float)(n - 1);
+        float ph = reduce_2pi(6.28318530718f * pb[0] * u * mj);
+        float s, c;
+        __sincosf(ph, &s, &c);
+        ctx += pa[j] * c;
+        stx += pa[j] * s;
+        crx += pa[n + j] * c;
+        srx += pa[n + j] * s;
+        wt += pa[j];
+        wr += pa[n + j];
+      }
+      float aft = sqrtf(ctx * ctx + stx * stx) / wt;
+      float afr = sqrtf(crx * crx + srx * srx) / wr;
+      return pb[1] * element_field32(ct, pb[2], pb[3]) * sqrtf(aft * afr);
+    }
+    case SS_PAT_FINITE_DIPOLE: {
+      float kh = 3.14159265359f * pa[0];
+      float ca = dot3f(dx, dy, dz, pv[0], pv[1], pv[2]);
+      float s = sqrtf(fmaxf(1.0f - ca * ca, 1e-12f));
+      float ck = __cosf(kh);
+      return __fdividef(fabsf(__cosf(kh * ca) - ck), s * (1.0f - ck));
+    }
+    case SS_PAT_TABULATED: {
+      float ct = fminf(fmaxf(dot3f(dx, dy, dz, pv[0], pv[1], pv[2]), -1.0f),
+                       1.0f);
+      float th = acosf(ct);
+      if (th <= pa[0]) return pb[0];
+      if (th >= pa[n - 1]) return pb[n - 1];
+      int lo = 0, hi = n - 1;
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (pa[mid] <= th) lo = mid; else hi = mid;
+      }
+      float slope = (pb[hi] - pb[lo]) / (pa[hi] - pa[lo]);
+      return __fmaf_rn(slope, th - pa[lo], pb[lo]);
+    }
+    default:
+      return 1.0f;
+  }
+}
+
+// Weideman w(z) in float32 (roughness.py:67-80).
+__device__ __forceinline__ void faddeeva32(const float *a, float L, float zr,
+                                           float zi, float &wr, float &wi) {
+  float dr = L + zi, di = -zr;
+  float nr = L - zi, ni = zr;
+  float inv = __fdividef(1.0f, dr * dr + di * di);
+  float Zr = (nr * dr + ni * di) * inv;
+  float Zi = (ni * dr - nr * di) * inv;
+  float pr = a[0], pi = 0.0f;
+#pragma unroll 8
+  for (int j = 1; j < SS_FAD_N; ++j) {
+    float tr = __fmaf_rn(pr, Zr, __fmaf_rn(-pi, Zi, a[j]));
+    pi = __fmaf_rn(pr, Zi, pi * Zr);
+    pr = tr;
+  }
+  float ir = dr * inv, ii = -di * inv;
+  float i2r = ir * ir - ii * ii, i2i = 2.0f * ir * ii;
+  wr = 2.0f * (pr * i2r - pi * i2i) + 0.564189583548f * ir;
+  wi = 2.0f * (pr * i2i + pi * i2r) + 0.564189583548f * ii;
+}
+
+__device__ __forceinline__ float f_factor32(const float *fa, float L, float m,
+                                            float a0, float edge, float l) {
+  float sq = sqrtf(m);
+  float x = a0 * l / (2.0f * sq);
+  float y = edge * sq / l;
+  float ex2 = __expf(-x * x), ey2 = __expf(-y * y);
+  float wzr, wzi, wxr, wxi;
+  faddeeva32(fa, L, x, y, wzr, wzi);
+  faddeeva32(fa, L, x, 0.0f, wxr, wxi);
+  float ae = reduce_2pi(a0 * edge);
+  float sr, cr;
+  __sincosf(ae, &sr, &cr);
+  float ar_ = x * cr - y * sr, ai_ = x * sr + y * cr;
+  float qi = ar_ * wzi + ai_ * wzr;
+  float t1 = -y * ex2 + ey2 * qi;
+  float t2 = x * wxi;
+  return 1.0f - ey2 * cr + 1.77245385091f * (t1 - t2);
+}
+
+// D_Phi in float32; lg[m] = lgamma(m + 1).
+template <int KIND>
+__device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
+                                         const float *fa, float fL,
+                                         float sigma, float l, float K,
+                                         float A0, float B0, float Lx,
+                                         float Ly) {
+  const float sk = sigma * K;
+  const float x = sk * sk;
+  if (!(x > 0.0f)) return 0.0f;
+  const float logx = __logf(x);
+  const float kb2 = A0 * A0 + B0 * B0;
+  float acc = 0.0f;
+  if (KIND == SS_ROUGH_GAUSS_AREA) {
+    const float c = 0.25f * kb2 * l * l;
+    const float pref = 3.14159265359f * l * l * Lx * Ly;
+    for (int m = 1; m <= n_terms; ++m) {
+      const float mf = (float)m;
+      const float im = __fdividef(1.0f, mf);
+      const float e = __fmaf_rn(mf, logx, -lg[m]) - x - c * im;
+      acc = __fmaf_rn(__expf(e), pref * im, acc);
+    }
+  } else if (KIND == SS_ROUGH_EXP_AREA) {
+    const float pref = 6.28318530718f * l * l * Lx * Ly;
+    const float kl2 = kb2 * l * l;
+    for (int m = 1; m <= n_terms; ++m) {
+      const float mf = (float)m;
+      const float im = __fdividef(1.0f, mf);
+      const float im2 = im * im;
+      const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
+      const float rs = rsqrtf(__fmaf_rn(kl2, im2, 1.0f));
+      acc = __fmaf_rn(__expf(e), pref * im2 * rs * rs * rs, acc);
+    }
+  } else {
+    const float l4 = (l * l) * (l * l);
+    for (int m = 1; m <= n_terms; ++m) {
+      const float mf = (float)m;
+      const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
+      const float w = __expf(e);
+      if (w == 0.0f) continue;
+      acc += w * (l4 / (mf * mf)) * f_factor32(fa, fL, mf, A0, Lx, l) *
+             f_factor32(fa, fL, mf, B0, Ly, l);
+    }
+  }
+  return fmaxf(acc, 0.0f);
+}
+
+struct SplitConsts {
+  float k, amp_pref, gamma, taper_inv;  // taper_inv = 1 / (2 s^2)
+  float K2h, K2l;                       // 2k as double-float
+  float Ah, Al, Bh, Bl;                 // u = r A - B, A = 2/(c dt), B = t0/dt
+  float fadL;
+  float sigma, corr;
+};
+
+template <int ROUGH>
+__global__ void __launch_bounds__(256)
+coherent_split_kernel(CoArgs a, SplitConsts k) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2 *hist = reinterpret_cast<float2 *>(smem_raw);
+  float *lg = reinterpret_cast<float *>(hist + (size_t)a.tb * a.n_seg);
+  __shared__ float s_ph[SS_MAX_TB][3], s_pl[SS_MAX_TB][3];
+  __shared__ double s_p64[SS_MAX_TB][3];
+  __shared__ float s_u[SS_MAX_TB][3];
+  __shared__ float s_pv[SS_MAX_TB][6];
+  __shared__ int s_lo[SS_MAX_TB], s_hi[SS_MAX_TB];
+  __shared__ float s_drop[SS_MAX_TB];
+  __shared__ float s_pat[SS_PAT_MAX];
+  __shared__ float s_fad[SS_FAD_N];
+  __shared__ int s_rng[2];
+
+  const int chunk = blockIdx.x;
+  const int t_base = blockIdx.y * a.tb;
+  const int nt = min(a.tb, a.T - t_base);
+  const int tid = threadIdx.x;
+  int pa_len = 0;
+  if (a.pat_kind == SS_PAT_ARRAY || a.pat_kind == SS_PAT_FINITE_DIPOLE)
+    pa_len = 1;
+  else if (a.pat_kind == SS_PAT_ARRAY_TAPERED)
+    pa_len = 2 * a.pat_n;
+  else if (a.pat_kind == SS_PAT_TABULATED)
+    pa_len = a.pat_n;
+  int pb_len = a.pat_kind == SS_PAT_TABULATED ? a.pat_n
+               : (a.pat_kind == SS_PAT_ARRAY ||
+                  a.pat_kind == SS_PAT_ARRAY_TAPERED) ? 4 : 0;
+
+  if (tid < nt) {
+    const int t = t_base + tid;
+    for (int j = 0; j < 3; ++j) {
+      const double pj = a.pos[3 * t + j];
+      const df v = df_from_double(pj);
+      s_ph[tid][j] = v.hi;
+      s_pl[tid][j] = v.lo;
+      s_p64[tid][j] = pj;
+      s_u[tid][j] = a.uct ? (float)a.uct[3 * t + j] : 0.0f;
+    }
+    for (int j = 0; j < 6; ++j)
+      s_pv[tid][j] =
+          (a.pv && j < a.pv_len) ? (float)a.pv[a.pv_len * t + j] : 0.0f;
+    long lo = (long)a.off[t] * a.bs;
+    long hi = min((long)(a.off[t] + a.n_win) * a.bs, (long)a.N);
+    s_lo[tid] = (int)min(lo, (long)a.N);
+    s_hi[tid] = (int)hi;
+    s_drop[tid] = 0.0f;
+  }
+  for (int j = tid; j < pa_len; j += blockDim.x) s_pat[j] = (float)a.pa[j];
+  for (int j = tid; j < pb_len; j += blockDim.x)
+    s_pat[pa_len + j] = (float)a.pb[j];
+  if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
+    s_fad[tid] = (float)a.fad.a[tid];
+  for (int j = tid; j < a.tb * a.n_seg; j += blockDim.x)
+    hist[j] = make_float2(0.0f, 0.0f);
+  if (ROUGH != SS_ROUGH_NONE)
+    for (int m = tid; m <= a.n_terms; m += blockDim.x)
+      lg[m] = (float)lgamma((double)m + 1.0);
+  __syncthreads();
+  if (tid == 0) {
+    int lo = s_lo[0], hi = s_hi[0];
+    for (int j = 1; j < nt; ++j) {
+      lo = min(lo, s_lo[j]);
+      hi = max(hi, s_hi[j]);
+    }
+    long len = max(hi - lo, 0);
+    s_rng[0] = lo + (int)(len * chunk / a.n_chunks);
+    s_rng[1] = lo + (int)(len * (chunk + 1) / a.n_chunks);
+  }
+  __syncthreads();
+
+  const float nsf = (float)a.n_samples;
+  for (int i = s_rng[0] + tid; i < s_rng[1]; i += blockDim.x) {
+    const float cx = a.F.cx[i], cy = a.F.cy[i], cz = a.F.cz[i];
+    const float nx = a.F.nx[i], ny = a.F.ny[i], nz = a.F.nz[i];
+    const float e1x = a.F.e1x[i], e1y = a.F.e1y[i], e1z = a.F.e1z[i];
+    const float e2x = a.F.e2x[i], e2y = a.F.e2y[i], e2z = a.F.e2z[i];
+    const float area = a.F.area[i];
+    const float gam = a.F.gamma_f32 ? a.F.gamma_f32[i] : k.gamma;
+    float sg = 0.f, lc = 0.f, phr = 0.f, phi = 0.f, l1 = 0.f, l2 = 0.f;
+    if (ROUGH != SS_ROUGH_NONE) {
+      sg = a.F.sigma ? a.F.sigma[i] : k.sigma;
+      lc = a.F.corr ? a.F.corr[i] : k.corr;
+      phr = a.F.phasor[2 * i];
+      phi = a.F.phasor[2 * i + 1];
+      l1 = sqrtf(dot3f(e1x, e1y, e1z, e1x, e1y, e1z));
+      l2 = sqrtf(dot3f(e2x, e2y, e2z, e2x, e2y, e2z));
+    }
+    for (int tt = 0; tt < nt; ++tt) {
+      if (i < s_lo[tt] || i >= s_hi[tt]) continue;
+      // --- d = p - c as double-float per component ---
+      float dxh, dxl, dyh, dyl, dzh, dzl, e;
+      two_sum(s_ph[tt][0], -cx, dxh, e);
+      fast_two_sum(dxh, e + s_pl[tt][0], dxh, dxl);
+      two_sum(s_ph[tt][1], -cy, dyh, e);
+      fast_two_sum(dyh, e + s_pl[tt][1], dyh, dyl);
+      two_sum(s_ph[tt][2], -cz, dzh, e);
+      fast_two_sum(dzh, e + s_pl[tt][2], dzh, dzl);
+      // --- S = |d|^2 (double-float) ---
+      float qx, ex, qy, ey, qz, ez;
+      two_prod(dxh, dxh, qx, ex);
+      two_prod(dyh, dyh, qy, ey);
+      two_prod(dzh, dzh, qz, ez);
+      float s1_, e1_, Sh, e2_;
+      two_sum(qx, qy, s1_, e1_);
+      two_sum(s1_, qz, Sh, e2_);
+      float Sl = (e1_ + e2_) + (ex + ey + ez) +
+                 2.0f * (dxh * dxl + dyh * dyl + dzh * dzl);
+      fast_two_sum(Sh, Sl, Sh, Sl);
+      // --- r = sqrt(S): rsqrt + one Newton correction ---
+      const float y = rsqrtf(Sh);
+      const float r0 = Sh * y;
+      const float res = __fmaf_rn(-r0, r0, Sh) + Sl;
+      float rh, rl;
+      fast_two_sum(r0, res * (0.5f * y), rh, rl);
+      const float inv_r = y;
+      // --- amplitude (float32) ---
+      const float rx = dxh * inv_r, ry = dyh * inv_r, rz = dzh * inv_r;
+      const float cosv = dot3f(rx, ry, rz, nx, ny, nz);
+      const float d1 = dot3f(rx, ry, rz, e1x, e1y, e1z);
+      const float d2 = dot3f(rx, ry, rz, e2x, e2y, e2z);
+      const float inv_r2 = inv_r * inv_r;
+      float amp = k.amp_pref * gam * cosv * area * sinc32(k.k * d1) *
+                  sinc32(k.k * d2) * inv_r2;
+      if (a.taper) {
+        float cc = fminf(fmaxf(cosv, 1e-9f), 1.0f);
+        float c2 = cc * cc;
+        amp *= __expf(-__fdividef(1.0f - c2, c2) * k.taper_inv);
+      }
+      float cr = amp, ci = 0.0f;
+      if (ROUGH != SS_ROUGH_NONE) {
+        const float kk = 2.0f * k.k * cosv;
+        const float dp = d_phi32<ROUGH>(a.n_terms, lg, s_fad, k.fadL, sg, lc,
+                                        kk, 2.0f * k.k * d1 / l1,
+                                        2.0f * k.k * d2 / l2, l1, l2);
+        const float amp_i =
+            area > 0.0f ? k.amp_pref * gam * cosv * inv_r2 * sqrtf(dp) : 0.0f;
+        const float sk = sg * kk;
+        const float att = __expf(-0.5f * sk * sk);
+        cr = amp * att + amp_i * phr;
+        ci = amp_i * phi;
+      }
+      // --- carrier phase 2 k r mod 2 pi (double-float) ---
+      float ph, pe;
+      two_prod(k.K2h, rh, ph, pe);
+      const float pl = pe + __fmaf_rn(k.K2h, rl, k.K2l * rh);
+      const float n2 = rintf(ph * 0.159154943091895336f);
+      float red = __fmaf_rn(-n2, 6.28318548202514648f, ph);  // exact
+      red = __fmaf_rn(-n2, -1.74845553146951e-07f, red) + pl;
+      float sn, cs;
+      __sincosf(red, &sn, &cs);
+      float re = cr * sn - ci * cs;
+      float im = cr * cs + ci * sn;
+      if (a.pat_kind != SS_PAT_ISOTROPIC) {
+        const float g = gain32(a.pat_kind, a.pat_n, pa_len, s_pat, s_pv[tt],
+                               -rx, -ry, -rz);
+        re *= g * g;
+        im *= g * g;
+      }
+      // --- bin: u = r A - B (double-float), exact re-bin near edges ---
+      float up, ue, us, ue2;
+      two_prod(rh, k.Ah, up, ue);
+      two_sum(up, -k.Bh, us, ue2);
+      const float ul = (ue2 + ue) + __fmaf_rn(rh, k.Al, rl * k.Ah) - k.Bl;
+      float fb = floorf(us);
+      float frac = (us - fb) + ul;
+      if (frac < 0.0f) { fb -= 1.0f; frac += 1.0f; }
+      else if (frac >= 1.0f) { fb += 1.0f; frac -= 1.0f; }
+      if ((frac < 1e-6f || frac > 0.999999f) && us > -4.0f &&
+          us < nsf + 4.0f) {
+        // float64 round-to-nearest chain, identical to the oracle
+        const double ddx = __dsub_rn(s_p64[tt][0], (double)cx);
+        const double ddy = __dsub_rn(s_p64[tt][1], (double)cy);
+        const double ddz = __dsub_rn(s_p64[tt][2], (double)cz);
+        const double rr = __dsqrt_rn(__dadd_rn(
+            __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)),
+            __dmul_rn(ddz, ddz)));
+        const double u64 = __ddiv_rn(
+            __dsub_rn(__ddiv_rn(__dmul_rn(2.0, rr), a.c), a.t0), a.dt);
+        const double f64b = floor(u64);
+        fb = (float)f64b;
+        frac = (float)(u64 - f64b);
+      }
+      int side_off = 0;
+      if (a.split &&
+          dot3f(-dxh, -dyh, -dzh, s_u[tt][0], s_u[tt][1], s_u[tt][2]) > 0.0f)
+        side_off = a.n_samples;
+      float2 *h = hist + (size_t)tt * a.n_seg + side_off;
+      if (a.interp) {
+        const float wq[2] = {1.0f - frac, frac};
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const float bq = fb + (float)q;
+          const float pr = re * wq[q], pim = im * wq[q];
+          if (bq >= 0.0f && bq < nsf) {
+            atomicAdd(&h[(int)bq].x, pr);
+            atomicAdd(&h[(int)bq].y, pim);
+          } else {
+            atomicAdd(&s_drop[tt], pr * pr + pim * pim);
+          }
+        }
+      } else if (fb >= 0.0f && fb < nsf) {
+        atomicAdd(&h[(int)fb].x, re);
+        atomicAdd(&h[(int)fb].y, im);
+      } else {
+        atomicAdd(&s_drop[tt], re * re + im * im);
+      }
+    }
+  }
+  __syncthreads();
+  float2 *part = reinterpret_cast<float2 *>(a.part);
+  for (int tt = 0; tt < nt; ++tt) {
+    const size_t base = ((size_t)chunk * a.T + t_base + tt) * a.n_seg;
+    for (int j = tid; j < a.n_seg; j += blockDim.x)
+      part[base + j] = hist[(size_t)tt * a.n_seg + j];
+  }
+  if (tid < nt)
+    a.part_drop[(size_t)chunk * a.T + t_base + tid] = (double)s_drop[tid];
+}
+
+int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st) {
+  int pa_len = 0, pb_len = 0;
+  if (a.pat_kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
+  if (a.pat_kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
+  if (a.pat_kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * a.pat_n; pb_len = 4; }
+  if (a.pat_kind == SS_PAT_TABULATED) { pa_len = a.pat_n; pb_len = a.pat_n; }
+  if (pa_len + pb_len > SS_PAT_MAX) {
+    set_error("antenna table too large for the split kernel");
+    return SS_ERR_UNSUPPORTED;
+  }
+  SplitConsts k{};
+  k.k = (float)a.k;
+  k.amp_pref = (float)(a.k / kTwoPi);
+  k.gamma = (float)a.gamma;
+  k.taper_inv = a.taper ? (float)(1.0 / (2.0 * a.taper_s * a.taper_s)) : 0.f;
+  const df k2 = df_from_double(2.0 * a.k);
+  k.K2h = k2.hi;
+  k.K2l = k2.lo;
+  const df A = df_from_double(2.0 / (a.c * a.dt));
+  const df B = df_from_double(a.t0 / a.dt);
+  k.Ah = A.hi;
+  k.Al = A.lo;
+  k.Bh = B.hi;
+  k.Bl = B.lo;
+  k.fadL = (float)a.fad.L;
+  k.sigma = (float)a.sigma;
+  k.corr = (float)a.corr;
+  dim3 grid(p.n_chunks, p.n_groups);
+  size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2) +
+                (a.rough_kind ? (a.n_terms + 1) * sizeof(float) : 0);
+  cudaError_t e = cudaSuccess;
+  switch (a.rough_kind) {
+#define SS_LAUNCH(R)                                                         \
+  case R:                                                                    \
+    e = cudaFuncSetAttribute(coherent_split_kernel<R>,                       \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                             (int)smem);                                     \
+    if (e != cudaSuccess) return cuda_status(e, "coherent_split smem");      \
+    coherent_split_kernel<R><<<grid, p.threads, smem, st>>>(a, k);           \
+    break;
+    SS_LAUNCH(SS_ROUGH_NONE)
+    SS_LAUNCH(SS_ROUGH_GAUSS_FULL)
+    SS_LAUNCH(SS_ROUGH_GAUSS_AREA)
+    SS_LAUNCH(SS_ROUGH_EXP_AREA)
+#undef SS_LAUNCH
+    default:
+      return SS_ERR_ARG;
+  }
+  return cuda_status(cudaGetLastError(), "coherent_split launch");
+}
+
+}  // namespace ss

@@ -1,0 +1,62 @@
+// Ordered reduction of per-CTA partial histograms into the output layout.
+#include "ss_internal.cuh"
+
+namespace ss {
+
+template <typename P>
+__global__ void chunk_reduce_kernel(ReduceArgs r, ss_output out) {
+  const P *part = reinterpret_cast<const P *>(r.part);
+  const long total = (long)r.T * r.n_seg;
+  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+       e += (long)gridDim.x * blockDim.x) {
+    const int t = (int)(e / r.n_seg);
+    const int b = (int)(e % r.n_seg);
+    double sr = 0.0, si = 0.0;
+    for (int c = 0; c < r.n_chunks; ++c) {
+      const P v = part[((size_t)c * r.T + t) * r.n_seg + b];
+      sr += (double)v.x;
+      si += (double)v.y;
+    }
+    long o = e;
+    if (r.split) {  // (T, 2, n) -> (T, n, 2) [left, right]
+      const int side = b / r.n_samples, bl = b % r.n_samples;
+      o = ((long)t * r.n_samples + bl) * 2 + side;
+    }
+    if (out.field_c128) {
+      out.field_c128[2 * o] = sr;
+      out.field_c128[2 * o + 1] = si;
+    } else {
+      out.field_c64[2 * o] = (float)sr;
+      out.field_c64[2 * o + 1] = (float)si;
+    }
+    if (b == 0) {
+      double d = 0.0;
+      for (int c = 0; c < r.n_chunks; ++c)
+        d += r.part_drop[(size_t)c * r.T + t];
+      out.dropped[t] = d;
+    }
+  }
+}
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+int launch_reduce(const ReduceArgs &r, bool f64_parts, const ss_output *out,
+                  cudaStream_t st) {
+  const int grid = 4 * sm_count();
+  if (f64_parts)
+    chunk_reduce_kernel<double2><<<grid, 256, 0, st>>>(r, *out);
+  else
+    chunk_reduce_kernel<float2><<<grid, 256, 0, st>>>(r, *out);
+  return cuda_status(cudaGetLastError(), "chunk_reduce launch");
+}
+
+}  // namespace ss

@@ -1,0 +1,34 @@
+// Refracted multilayer kernel: argument block (internal).
+#pragma once
+
+#include "ss_internal.cuh"
+
+namespace ss {
+
+struct RefArgs {
+  ss_facets F;
+  const double *pos, *uct, *pv;
+  const int32_t *off;
+  int T, N, pv_len;
+  // crossed stack (top-down, joint pads first)
+  int ni, k_pad;
+  ss_interface ifc[SS_MAX_IFACE];
+  double n_leg[SS_MAX_IFACE + 1], eps_leg[SS_MAX_IFACE + 1],
+      att_leg[SS_MAX_IFACE + 1], sig_c[SS_MAX_IFACE];
+  int rough_cross;
+  double k0, gamma, t0, dt, c, taper_s, n_exp;
+  int n_samples, n_seg, bs, n_win, split, coherent, joint, n_newton,
+      n_backtrack, taper, precision;
+  int pat_kind, pat_n;
+  const double *pa, *pb;
+  int rough_kind, n_terms;
+  double sigma, corr;
+  FadCoeffs fad;
+  int tb, n_chunks;
+  void *part;
+  double *part_drop;
+};
+
+int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st);
+
+}  // namespace ss

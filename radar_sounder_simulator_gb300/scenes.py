@@ -1,0 +1,170 @@
+"""Seeded synthetic scenes for the benchmark configurations and tests.
+
+Host-side inputs only (no kernel code). Facets follow the reference's corner
+rule for rectangular DEM cells (soundersim ``scene.py:156-166``): mean edge
+vectors e1 (along +column) and e2 (along +row), centroid = mean of the four
+corners, area = |e1 x e2|, normal = (e1 x e2)/area oriented +z. Surfaces are
+Gaussian random fields with an isotropic Gaussian (``compare/haynes.py``
+generator form) or exponential correlation function, built by circular FFT
+filtering of white noise and normalised by the filter's energy so the field
+variance is exactly the target (no per-realisation rescaling).
+"""
+
+from types import SimpleNamespace
+
+import numpy as np
+
+C_LIGHT = 299792458.0
+
+
+def random_field(n, dx, corr_len, rms, rng, acf="exponential"):
+    """(n, n) zero-mean random field with rms ``rms`` and the given ACF."""
+    kx = 2.0 * np.pi * np.fft.fftfreq(n, d=dx)
+    k2 = kx[:, None] ** 2 + kx[None, :] ** 2
+    if acf == "exponential":
+        # 2-D spectrum of exp(-r/l): 2 pi l^2 (1 + k^2 l^2)^(-3/2)
+        spec = 2.0 * np.pi * corr_len ** 2 * (1.0 + k2 * corr_len ** 2) ** -1.5
+    elif acf == "gaussian":
+        # 2-D spectrum of exp(-r^2/l^2): pi l^2 exp(-k^2 l^2 / 4)
+        spec = np.pi * corr_len ** 2 * np.exp(-k2 * corr_len ** 2 / 4.0)
+    else:
+        raise ValueError(f"unknown acf {acf!r}")
+    h = np.sqrt(spec)
+    w = rng.standard_normal((n, n))
+    z = np.real(np.fft.ifft2(np.fft.fft2(w) * h))
+    return rms * z / np.sqrt(np.mean(h * h))
+
+
+def facets_from_vertices(X, Y, Z):
+    """Rectangular facets of a vertex grid (scene.py:156-166 corner rule).
+    Returns a Facets-like namespace with ``cell`` and ``grid_shape`` for the
+    refracted kernel's lookup tables."""
+    V = np.stack([X, Y, Z], axis=-1)
+    v00, v01 = V[:-1, :-1], V[:-1, 1:]
+    v10, v11 = V[1:, :-1], V[1:, 1:]
+    e1 = ((v01 + v11) - (v00 + v10)) / 2.0
+    e2 = ((v10 + v11) - (v00 + v01)) / 2.0
+    centers = ((v00 + v01 + v10 + v11) / 4.0).reshape(-1, 3)
+    raw = np.cross(e1, e2).reshape(-1, 3)
+    areas = np.linalg.norm(raw, axis=1)
+    normals = raw / areas[:, None]
+    normals *= np.where(normals[:, 2] < 0.0, -1.0, 1.0)[:, None]
+    ny, nx = X.shape[0] - 1, X.shape[1] - 1
+    ci, cj = np.meshgrid(np.arange(ny), np.arange(nx), indexing="ij")
+    return SimpleNamespace(
+        centers=centers, normals=normals, areas=areas,
+        e1=e1.reshape(-1, 3), e2=e2.reshape(-1, 3),
+        cell=np.stack([ci.ravel(), cj.ravel()], axis=1), grid_shape=(ny, nx),
+        phase_keys=None)
+
+
+def surface(n_cells, spacing, rms, corr_len, z0, rng, acf="exponential"):
+    """Square patch of n_cells^2 facets centred on the origin."""
+    ax = (np.arange(n_cells + 1) - n_cells / 2.0) * spacing
+    X, Y = np.meshgrid(ax, ax)
+    Z = z0 + random_field(n_cells + 1, spacing, corr_len, rms, rng, acf)
+    return facets_from_vertices(X, Y, Z)
+
+
+def straight_track(n, spacing, altitude):
+    """Track along +x through the origin; u_ct = (0, -1, 0) (nav.py:25-29:
+    cross-track-right of +x travel in an ENU frame)."""
+    x = (np.arange(n) - (n - 1) / 2.0) * spacing
+    pos = np.column_stack([x, np.zeros(n), np.full(n, float(altitude))])
+    uct = np.tile([0.0, -1.0, 0.0], (n, 1))
+    return pos, uct
+
+
+def fresnel_normal(eps1, eps2):
+    """Normal-incidence field reflection (physics.py:16-21)."""
+    n1, n2 = np.sqrt(eps1), np.sqrt(eps2)
+    return (n1 - n2) / (n1 + n2)
+
+
+def eps_kovacs(rho):
+    """Kovacs density -> permittivity (firn.py:19-21)."""
+    return (1.0 + 0.845 * np.asarray(rho) / 1000.0) ** 2
+
+
+def firn_n_eff(depth, rho_surface=350.0, rho_ice=917.0, scale=30.0):
+    """Delay-equivalent index of the firn column over ``depth`` metres:
+    (1/depth) int_0^depth sqrt(eps(rho(z))) dz with rho(z) = rho_ice -
+    (rho_ice - rho_surface) exp(-z/scale)."""
+    z = np.linspace(0.0, depth, 20001)
+    rho = rho_ice - (rho_ice - rho_surface) * np.exp(-z / scale)
+    n = np.sqrt(eps_kovacs(rho))
+    return float(np.trapezoid(n, z) / depth)
+
+
+def window(pos, centers, *, n_samples, dt, lead_m=200.0, c=C_LIGHT):
+    """t0 = 2 (min slant range - lead) / c (the configs' window rule)."""
+    r = np.linalg.norm(pos[:, None, :] - centers[None, ::97], axis=-1).min()
+    return 2.0 * (r - lead_m) / c
+
+
+def config1(seed=1):
+    """Plain single-surface coherent run: 128^2 facets of 100 m,
+    exponential ACF (1 km, 50 m rms), air/ice (eps 3.15) Fresnel, isotropic
+    antenna, 256 traces at 50 m, 20 km altitude, 60 MHz, dt = 1/(2 x 15 MHz),
+    2048 bins."""
+    rng = np.random.default_rng(seed)
+    f = surface(128, 100.0, 50.0, 1000.0, 0.0, rng)
+    pos, uct = straight_track(256, 50.0, 20000.0)
+    f0, bw = 60e6, 15e6
+    dt = 1.0 / (2.0 * bw)
+    t0 = window(pos, f.centers, n_samples=2048, dt=dt)
+    kw = dict(k=2 * np.pi * f0 / C_LIGHT, gamma=fresnel_normal(1.0, 3.15),
+              t0=t0, dt=dt, n_samples=2048, c=C_LIGHT)
+    return SimpleNamespace(facets=f, pos=pos, uct=uct, kw=kw, f0=f0, bw=bw,
+                           pulse_length=20e-6)
+
+
+def config2(seed=2, n_cells=512, n_traces=1024, spacing=50.0,
+            trace_spacing=25.0):
+    """Multilayer with refraction: surface + horizons at 300 m and 1200 m +
+    bed at 2500 m, each n_cells^2 facets of ``spacing`` metres; 1024 traces
+    at 20 km; 60 MHz / 15 MHz.
+
+    Choices where the configuration is silent (recorded in the design doc):
+    horizon ACF exponential with 1 km correlation; bed relief exponential,
+    5 km; relative permittivity contrast 1e-3 at both horizons (their target
+    reflection coefficient fresnel_normal(eps, eps (1 + 1e-3))); firn column
+    above the first horizon as one medium of delay-equivalent index; 25 m
+    trace spacing; bed reflectivity +10^(R/20) with R ~ U[-30, -5] dB."""
+    rng = np.random.default_rng(seed)
+    surf = surface(n_cells, spacing, 20.0, 5000.0, 0.0, rng)
+    h1 = surface(n_cells, spacing, 5.0, 1000.0, -300.0, rng)
+    h2 = surface(n_cells, spacing, 5.0, 1000.0, -1200.0, rng)
+    bed = surface(n_cells, spacing, 300.0, 5000.0, -2500.0, rng)
+    pos, uct = straight_track(n_traces, trace_spacing, 20000.0)
+    n_firn = firn_n_eff(300.0)
+    eps_ice = 3.15
+    eps = [1.0, n_firn ** 2, eps_ice, eps_ice * (1.0 + 1e-3),
+           eps_ice * (1.0 + 1e-3) ** 2]
+    att = [0.0, 10.0, 10.0, 10.0, 10.0]
+    f0, bw = 60e6, 15e6
+    dt = 1.0 / (2.0 * bw)
+    t0 = window(pos, surf.centers, n_samples=2048, dt=dt)
+    r_db = rng.uniform(-30.0, -5.0, len(bed.centers))
+    gammas = [fresnel_normal(eps[0], eps[1]),
+              fresnel_normal(eps_ice, eps_ice * (1.0 + 1e-3)),
+              fresnel_normal(eps[2], eps[3]),
+              10.0 ** (r_db / 20.0)]
+    return SimpleNamespace(
+        layers=[surf, h1, h2, bed], names=["surface", "h1", "h2", "bed"],
+        pos=pos, uct=uct, eps=eps, att=att, gammas=gammas, f0=f0, bw=bw,
+        k0=2 * np.pi * f0 / C_LIGHT, t0=t0, dt=dt, n_samples=2048,
+        c=C_LIGHT, refraction="joint")
+
+
+def smoke_scene():
+    """Tiny coherent case for ``__graft_entry__.smoke``."""
+    rng = np.random.default_rng(7)
+    f = surface(24, 30.0, 2.0, 200.0, 0.0, rng)
+    pos, uct = straight_track(4, 40.0, 2000.0)
+    dt = 2e-8
+    t0 = window(pos, f.centers, n_samples=256, dt=dt, lead_m=20.0)
+    kw = dict(k=2 * np.pi / 5.0, gamma=-0.28, t0=t0, dt=dt, n_samples=256,
+              c=C_LIGHT)
+    return dict(pos=pos, uct=uct, centers=f.centers, normals=f.normals,
+                areas=f.areas, e1=f.e1, e2=f.e2, kw=kw)
