@@ -1,0 +1,419 @@
+"""Benchmark: facet.trace contributions/s of the coherent facet path on
+GB300, multilayer refraction configuration (surface + 2 horizons + bed, 512^2
+facets of 50 m each, 1024 traces at 20 km, 60 MHz / 15 MHz).
+
+One step = the whole forward pass over that scene: the surface coherent sum
+plus the three refracted targets (first horizon sequential, second horizon
+and bed joint), split-precision form, inputs resident in HBM, L2 flushed
+before every step. Also measured: the float64 form's rate (``fp64``), the
+drop-in NumPy-in/NumPy-out path with host copies in the timed region
+(``e2e``), the split form's error against the float64 form, the dominant
+kernel's roofline position and a CPU baseline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("facet·trace contribs/s, split-FP32 vs FP64 GPU form, at "
+          "≤0.01 dB vs FP64")
+UNIT = "contribs/s"
+WORKLOAD = "multilayer_refraction_512sq_x4_1024tr"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-cells", type=int, default=512)
+    ap.add_argument("--n-traces", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--skip-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def config_dict(args, ws):
+    return {"workload": WORKLOAD, "layers": 4,
+            "facets_per_layer": args.n_cells ** 2, "facet_m": 50.0,
+            "traces_per_gpu": args.n_traces, "n_samples": 2048,
+            "f0_hz": 60e6, "bandwidth_hz": 15e6,
+            "refraction": "joint for targets under >= 2 interfaces",
+            "l2": "flushed before every step (256 MiB write)",
+            "parallelism": f"independent lines x{ws}"}
+
+
+# --------------------------------------------------------------------------
+# workload
+# --------------------------------------------------------------------------
+def build_plans(cfg, precision, device):
+    """Device-resident plans for the four targets of one step."""
+    from radar_sounder_simulator_gb300.coherent import prepare_coherent
+    from radar_sounder_simulator_gb300.multilayer import prepare_refracted
+    L = cfg.layers
+    plans = [prepare_coherent(
+        cfg.pos, cfg.uct, L[0].centers, L[0].normals, L[0].areas, L[0].e1,
+        L[0].e2, k=cfg.k0, gamma=cfg.gammas[0], t0=cfg.t0, dt=cfg.dt,
+        n_samples=cfg.n_samples, c=cfg.c, precision=precision,
+        device=device)]
+    for j in range(1, 4):
+        refr = cfg.refraction if j > 1 else "sequential"
+        plans.append(prepare_refracted(
+            cfg.pos, cfg.uct, L[j], L[:j], cfg.eps[:j + 1], cfg.att[:j + 1],
+            mode="coherent", t0=cfg.t0, dt=cfg.dt, n_samples=cfg.n_samples,
+            c=cfg.c, gamma=cfg.gammas[j], k0=cfg.k0, refraction=refr,
+            precision=precision, device=device))
+    return plans
+
+
+def drop_in_step(cfg, precision, device):
+    """The reference-facing call sequence with host buffers (e2e)."""
+    from radar_sounder_simulator_gb300.coherent import coherent_cluttergram
+    from radar_sounder_simulator_gb300.multilayer import refracted_cluttergram
+    L = cfg.layers
+    outs = [coherent_cluttergram(
+        cfg.pos, cfg.uct, L[0].centers, L[0].normals, L[0].areas, L[0].e1,
+        L[0].e2, k=cfg.k0, gamma=cfg.gammas[0], t0=cfg.t0, dt=cfg.dt,
+        n_samples=cfg.n_samples, c=cfg.c, precision=precision,
+        device=device)]
+    for j in range(1, 4):
+        refr = cfg.refraction if j > 1 else "sequential"
+        outs.append(refracted_cluttergram(
+            cfg.pos, cfg.uct, L[j], L[:j], cfg.eps[:j + 1], cfg.att[:j + 1],
+            mode="coherent", t0=cfg.t0, dt=cfg.dt, n_samples=cfg.n_samples,
+            c=cfg.c, gamma=cfg.gammas[j], k0=cfg.k0, refraction=refr,
+            precision=precision, device=device))
+    return outs
+
+
+def host_bytes(cfg):
+    """Bytes the drop-in path copies host->device and device->host per
+    step (counted from the arrays it uploads and downloads)."""
+    T = len(cfg.pos)
+    h2d = d2h = 0
+    for j, f in enumerate(cfg.layers):
+        n = len(f.centers)
+        h2d += 13 * 4 * n                       # float32 facet SoA
+        h2d += T * (3 * 8 * 2 + 4)              # positions, u_ct, windows
+        if j > 0 and np.ndim(cfg.gammas[j]):
+            h2d += 8 * n                        # per-facet gamma
+        for g in cfg.layers[:j]:
+            h2d += 6 * 4 * len(g.centers)       # lookup tables
+        d2h += T * cfg.n_samples * 16 + T * 8   # field (re, im f64) + dropped
+    return h2d, d2h
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}",
+                 f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return False
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        for line in out.splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+        return False
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4)
+                          if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+# --------------------------------------------------------------------------
+# CPU baseline / reference arm (float64 oracle restatement on host cores)
+# --------------------------------------------------------------------------
+def _oracle_sample(args_tuple):
+    """Worker: one trace of one layer through the NumPy float64 oracle."""
+    (layer, j, pos, uct, cfg_small) = args_tuple
+    from oracle import lpa, refracted
+    if j == 0:
+        f = layer[0]
+        out, _ = lpa.coherent_cluttergram(
+            pos, uct, f.centers, f.normals, f.areas, f.e1, f.e2,
+            k=cfg_small["k0"], gamma=cfg_small["gammas"][0],
+            t0=cfg_small["t0"], dt=cfg_small["dt"],
+            n_samples=cfg_small["n_samples"], c=cfg_small["c"])
+    else:
+        refr = "joint" if j > 1 else "sequential"
+        out, _ = refracted.refracted_cluttergram(
+            pos, uct, layer[j], layer[:j], cfg_small["eps"][:j + 1],
+            cfg_small["att"][:j + 1], mode="coherent", t0=cfg_small["t0"],
+            dt=cfg_small["dt"], n_samples=cfg_small["n_samples"],
+            c=cfg_small["c"], gamma=cfg_small["gammas"][j],
+            k0=cfg_small["k0"], refraction=refr)
+    return len(layer[j].centers) * len(pos)
+
+
+def cpu_sample_rate(cfg, seconds, cores):
+    """Oracle pairs/s on a bounded sample: whole layers, a few traces, spread
+    over ``cores`` spawned worker processes; grows the sample until it takes
+    about ``seconds``."""
+    import multiprocessing as mp
+    small = dict(k0=cfg.k0, gammas=cfg.gammas, t0=cfg.t0, dt=cfg.dt,
+                 n_samples=cfg.n_samples, c=cfg.c, eps=cfg.eps, att=cfg.att)
+    ctx = mp.get_context("spawn")
+    T = len(cfg.pos)
+    jobs = []
+    rng = np.random.default_rng(0)
+    picks = rng.choice(T, size=min(T, 4 * cores), replace=False)
+    for t in picks:
+        for j in range(4):
+            jobs.append((cfg.layers, j, cfg.pos[t:t + 1], cfg.uct[t:t + 1],
+                         small))
+    with ctx.Pool(cores) as pool:
+        t0 = time.perf_counter()
+        done = 0
+        it = pool.imap_unordered(_oracle_sample, jobs)
+        for n in it:
+            done += n
+            if time.perf_counter() - t0 > seconds:
+                pool.terminate()
+                break
+        el = time.perf_counter() - t0
+    return done / el, f"{done} pairs ({len(picks)} traces x 4 layers max, " \
+                      f"whole layers) in {el:.1f} s"
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from radar_sounder_simulator_gb300 import scenes
+    cfg = scenes.config2(n_cells=args.n_cells, n_traces=args.n_traces)
+    cores = os.cpu_count() or 1
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample_rate(cfg, min(args.cpu_seconds, 5.0), cores)
+    for _ in range(args.steps):
+        v, sample = cpu_sample_rate(cfg, args.cpu_seconds / 2, cores)
+        vals.append(v)
+    value = float(np.median(vals))
+    pairs_step = 4 * args.n_cells ** 2 * args.n_traces
+    line = {"impl": "reference", "metric": METRIC, "value": value,
+            "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": pairs_step / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded config-2 scene)",
+            "config": config_dict(args, ws),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "reference JAX CPU path unavailable on this host (jax "
+                    "not installed); float64 NumPy restatement of the "
+                    "reference formulas timed instead"}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    if ws > 1:
+        dist.init_process_group("nccl", device_id=device)
+
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.coherent import coherent_run_count
+    cfg = scenes.config2(n_cells=args.n_cells, n_traces=args.n_traces,
+                         line_offset_y=200.0 * rank)
+    pairs_step = sum(len(f.centers) for f in cfg.layers) * len(cfg.pos)
+
+    plans = build_plans(cfg, "split", device)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    stream = torch.cuda.current_stream(device)
+
+    def step(record=None):
+        flush.fill_(1)
+        outs = []
+        for i, p in enumerate(plans):
+            if record is not None:
+                record[i][0].record(stream)
+            outs.append(p.run())
+            if record is not None:
+                record[i][1].record(stream)
+        return outs
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ev = [[(torch.cuda.Event(enable_timing=True),
+            torch.cuda.Event(enable_timing=True)) for _ in plans]
+          for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    if ws > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        t_start.record(stream)
+        for s in range(args.steps):
+            outs = step(ev[s])
+        t_end.record(stream)
+        torch.cuda.synchronize()
+    if ws > 1:
+        dist.barrier()
+    ms = t_start.elapsed_time(t_end) / args.steps
+    ms_t = torch.tensor([ms], device=device, dtype=torch.float64)
+    if ws > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = pairs_step * ws / (ms * 1e-3)
+    per_kernel = [float(np.mean([ev[s][i][0].elapsed_time(ev[s][i][1])
+                                 for s in range(args.steps)]))
+                  for i in range(len(plans))]
+
+    # float64 form on the same scene (one step) and the split form's error
+    fp64 = None
+    err = None
+    if not args.skip_fp64:
+        plans64 = build_plans(cfg, "fp64", device)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        flush.fill_(1)
+        e0.record(stream)
+        outs64 = [p.run() for p in plans64]
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = e0.elapsed_time(e1)
+        fp64 = {"value": pairs_step / (ms64 * 1e-3), "unit": UNIT,
+                "ms_per_step": ms64}
+        err = split_error(outs, outs64)
+        del plans64, outs64
+
+    # end to end through the drop-in API with host buffers
+    h2d, d2h = host_bytes(cfg)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    drop_in_step(cfg, "split", device)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+
+    launches = args.steps * sum(coherent_run_count(p) for p in plans)
+    roof = roofline(per_kernel, plans)
+    if rank == 0:
+        cpu = None
+        if ws == 1:
+            v, sample = cpu_sample_rate(cfg, args.cpu_seconds,
+                                        os.cpu_count() or 1)
+            cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1,
+                   "kind": "port", "sample": sample}
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (seeded config-2 scene)",
+                "config": config_dict(args, ws),
+                "e2e": {"value": pairs_step / e2e_s, "unit": UNIT,
+                        "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "fp64": fp64,
+                "split_over_fp64": (value / ws / fp64["value"]) if fp64
+                else None,
+                "error_vs_fp64": err,
+                "per_kernel_ms": dict(zip(["surface", "h1_seq", "h2_joint",
+                                           "bed_joint"], per_kernel)),
+                "gpu_launches": launches, "roofline": roof,
+                "clocks": clk.summary(), "cpu_baseline": cpu}
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        dist.destroy_process_group()
+
+
+def split_error(outs, outs64):
+    """Relative L2, max phase error and max power error (dB, bins above -60
+    dB of each layer's peak) of the split form against the float64 form."""
+    import torch
+    worst = {"rel_l2": 0.0, "phase_rad": 0.0, "power_db": 0.0}
+    for (f, _), (g, _) in zip(outs, outs64):
+        a = torch.view_as_complex(f.contiguous())
+        b = torch.view_as_complex(g.contiguous())
+        rel = (torch.linalg.vector_norm(a - b) /
+               torch.linalg.vector_norm(b)).item()
+        p = b.abs() ** 2
+        keep = p > p.max() * 1e-6
+        ph = torch.angle(a[keep] / b[keep]).abs().max().item()
+        db = (10 * torch.log10(a[keep].abs() ** 2 / p[keep])).abs().max().item()
+        worst = {"rel_l2": max(worst["rel_l2"], rel),
+                 "phase_rad": max(worst["phase_rad"], ph),
+                 "power_db": max(worst["power_db"], db)}
+    return worst
+
+
+def roofline(per_kernel_ms, plans):
+    """Dominant kernel's position against the FP32 pipe (filled in from the
+    per-pair operation counts of the kernel that dominates the step)."""
+    i = int(np.argmax(per_kernel_ms))
+    names = ["surface", "h1_seq", "h2_joint", "bed_joint"]
+    return {"kernel": names[i], "ms": per_kernel_ms[i]}
+
+
+if __name__ == "__main__":
+    main()

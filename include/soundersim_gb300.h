@@ -174,10 +174,15 @@ typedef struct {
 typedef struct {
   int32_t n_crossed;             /* crossed interfaces incl. joint pads     */
   int32_t k_pad;                 /* leading no-op pads (joint only)         */
+  int32_t n_legs;                /* entries in the leg arrays: crossing i
+                                    uses [i] and [i + 1], the final leg the
+                                    last entry (multilayer.py:506-508 reads
+                                    n_leg[-1] / att[-1]); >= n_crossed + 1,
+                                    == n_crossed + 1 for the joint solve    */
   const ss_interface *crossed;   /* (host) n_crossed descriptors, top-down  */
-  const double *n_leg;           /* (host) n_crossed + 1 refractive indices */
-  const double *eps_leg;         /* (host) n_crossed + 1 permittivities     */
-  const double *att_leg;         /* (host) n_crossed + 1 one-way dB/km      */
+  const double *n_leg;           /* (host) n_legs refractive indices        */
+  const double *eps_leg;         /* (host) n_legs permittivities            */
+  const double *att_leg;         /* (host) n_legs one-way dB/km             */
   const double *sigma_crossed;   /* (host) n_crossed rms heights, or NULL   */
   double k0, gamma, t0, dt, c;
   double taper_s;                /* used when taper != 0                    */

@@ -59,6 +59,29 @@ class Output(C.Structure):
                 ("dropped", C.c_void_p)]
 
 
+class Interface(C.Structure):
+    _fields_ = [("table", C.c_void_p), ("ny", C.c_int32), ("nx", C.c_int32),
+                ("coef", C.c_double * 6), ("mean_point", C.c_double * 3),
+                ("mean_normal", C.c_double * 3)]
+
+
+class RefractedOpts(C.Structure):
+    _fields_ = [("n_crossed", C.c_int32), ("k_pad", C.c_int32),
+                ("n_legs", C.c_int32), ("crossed", C.POINTER(Interface)),
+                ("n_leg", C.POINTER(C.c_double)),
+                ("eps_leg", C.POINTER(C.c_double)),
+                ("att_leg", C.POINTER(C.c_double)),
+                ("sigma_crossed", C.POINTER(C.c_double)),
+                ("k0", C.c_double), ("gamma", C.c_double),
+                ("t0", C.c_double), ("dt", C.c_double), ("c", C.c_double),
+                ("taper_s", C.c_double), ("diffuse_exp", C.c_double),
+                ("n_samples", C.c_int32), ("block_size", C.c_int32),
+                ("n_win", C.c_int32), ("split_sides", C.c_int32),
+                ("coherent", C.c_int32), ("joint", C.c_int32),
+                ("joint_newton", C.c_int32), ("joint_backtrack", C.c_int32),
+                ("taper", C.c_int32), ("precision", C.c_int32)]
+
+
 # entry point name -> (restype, argtypes); the ABI surface the tests check
 SIGNATURES = {
     "ss_coherent_scratch_bytes": (C.c_size_t, [C.POINTER(CoherentOpts),
@@ -67,6 +90,13 @@ SIGNATURES = {
                                   C.POINTER(Traces), C.POINTER(Pattern),
                                   C.POINTER(Roughness), C.POINTER(Output),
                                   C.c_void_p, C.c_size_t, C.c_void_p]),
+    "ss_refracted_scratch_bytes": (C.c_size_t, [C.POINTER(RefractedOpts),
+                                                C.c_int32, C.c_int32]),
+    "ss_refracted_fwd": (C.c_int, [C.POINTER(RefractedOpts),
+                                   C.POINTER(Facets), C.POINTER(Traces),
+                                   C.POINTER(Pattern), C.POINTER(Roughness),
+                                   C.POINTER(Output), C.c_void_p, C.c_size_t,
+                                   C.c_void_p]),
     "ss_version": (C.c_char_p, []),
     "ss_last_error": (C.c_char_p, []),
 }

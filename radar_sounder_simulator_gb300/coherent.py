@@ -125,17 +125,60 @@ def rough_struct(roughness, d_phi_area):
     return st, s_arr, l_arr, phasors
 
 
-def coherent_cluttergram(positions, u_ct, centers, normals, areas, e1, e2, *,
-                         k, gamma, t0, dt, n_samples, c, split_sides=False,
-                         interp_bins=False, pattern=None, roughness=None,
-                         taper_s=None, d_phi_area=False, block_size=None,
-                         window_cull=True, precision="fp64",
-                         out_dtype=np.complex64, device=None):
-    """Binned coherent field for every trace (coherent.py:247-362).
+class CoherentPlan:
+    """Device-resident inputs of one coherent_cluttergram call."""
 
-    Returns ``(field, dropped)``: field (T, n_samples) or (T, n_samples, 2)
-    [left, right] with the absolute carrier phase, dropped (T,) float32
-    out-of-window power."""
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
+
+    def run(self, precision=None, out=None):
+        """Launch on the current stream; returns device tensors (field
+        (T, n_seg, 2) float64 re/im in the output layout, dropped (T,))."""
+        self.opts.precision = _lib.PREC[precision or self.precision]
+        L = _lib.lib()
+        nbytes = L.ss_coherent_scratch_bytes(C.byref(self.opts), self.T,
+                                             self.N)
+        if nbytes == 0:
+            raise ValueError("unsupported sizes for the coherent kernel")
+        if self.scratch is None or self.scratch.numel() < nbytes:
+            self.scratch = torch.empty(nbytes, dtype=torch.uint8,
+                                       device=self.device)
+        if out is None:
+            field = torch.empty((self.T, self.n_seg, 2), dtype=torch.float64,
+                                device=self.device)
+            dropped = torch.empty(self.T, dtype=torch.float64,
+                                  device=self.device)
+        else:
+            field, dropped = out
+        o = _lib.Output(field.data_ptr(), None, dropped.data_ptr())
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        st = L.ss_coherent_fwd(C.byref(self.opts), C.byref(self.fst),
+                               C.byref(self.tr), C.byref(self.pst),
+                               C.byref(self.rst), C.byref(o),
+                               C.c_void_p(self.scratch.data_ptr()), nbytes,
+                               C.c_void_p(stream))
+        _lib.check(st, "ss_coherent_fwd")
+        return field, dropped
+
+    def to_numpy(self, field, dropped, out_dtype=np.complex64):
+        f = field.cpu().numpy()
+        res = (f[..., 0] + 1j * f[..., 1]).astype(out_dtype)
+        if self.split:
+            res = res.reshape(self.T, self.n_samples, 2)
+        return res, dropped.cpu().numpy().astype(np.float32)
+
+
+def coherent_run_count(plan):
+    """Library kernels one ``run()`` launches (main pass + chunk reduce)."""
+    return 2
+
+
+def prepare_coherent(positions, u_ct, centers, normals, areas, e1, e2, *, k,
+                     gamma, t0, dt, n_samples, c, split_sides=False,
+                     interp_bins=False, pattern=None, roughness=None,
+                     taper_s=None, d_phi_area=False, block_size=None,
+                     window_cull=True, precision="fp64", device=None):
+    """Host preparation of coherent.py:284-348 and the device upload."""
     device = torch.device(device or "cuda")
     pos = np.asarray(positions, np.float64)
     T = len(pos)
@@ -164,25 +207,31 @@ def coherent_cluttergram(positions, u_ct, centers, normals, areas, e1, e2, *,
         float(c), float(taper_s or 0.0), int(n_samples), plan.block_size,
         plan.n_win, int(bool(split_sides)), int(bool(interp_bins)),
         int(taper_s is not None), _lib.PREC[precision])
-    L = _lib.lib()
-    nbytes = L.ss_coherent_scratch_bytes(C.byref(opts), T, n)
-    if nbytes == 0:
-        raise ValueError("unsupported sizes for the coherent kernel")
-    scratch = torch.empty(nbytes, dtype=torch.uint8, device=device)
-    n_seg = n_samples * (2 if split_sides else 1)
-    field = torch.empty((T, n_seg, 2), dtype=torch.float64, device=device)
-    dropped = torch.empty(T, dtype=torch.float64, device=device)
-    out = _lib.Output(field.data_ptr(), None, dropped.data_ptr())
-    fst = fac.struct()
-    stream = torch.cuda.current_stream(device).cuda_stream
-    st = L.ss_coherent_fwd(C.byref(opts), C.byref(fst), C.byref(tr),
-                           C.byref(pst), C.byref(rst), C.byref(out),
-                           C.c_void_p(scratch.data_ptr()), nbytes,
-                           C.c_void_p(stream))
-    _lib.check(st, "ss_coherent_fwd")
-    f = field.cpu().numpy()
-    res = (f[..., 0] + 1j * f[..., 1]).astype(out_dtype)
-    if split_sides:
-        res = res.reshape(T, n_samples, 2)
-    del keep
-    return res, dropped.cpu().numpy().astype(np.float32)
+    return CoherentPlan(
+        opts=opts, fst=fac.struct(), tr=tr, pst=pst, rst=rst,
+        keep=[fac, keep, pos_t, uct_t, off_t, pv_t], T=T, N=n,
+        n_samples=int(n_samples),
+        n_seg=int(n_samples) * (2 if split_sides else 1),
+        split=bool(split_sides), device=device, precision=precision,
+        scratch=None, cull=plan)
+
+
+def coherent_cluttergram(positions, u_ct, centers, normals, areas, e1, e2, *,
+                         k, gamma, t0, dt, n_samples, c, split_sides=False,
+                         interp_bins=False, pattern=None, roughness=None,
+                         taper_s=None, d_phi_area=False, block_size=None,
+                         window_cull=True, precision="fp64",
+                         out_dtype=np.complex64, device=None):
+    """Binned coherent field for every trace (coherent.py:247-362).
+
+    Returns ``(field, dropped)``: field (T, n_samples) or (T, n_samples, 2)
+    [left, right] with the absolute carrier phase, dropped (T,) float32
+    out-of-window power."""
+    plan = prepare_coherent(
+        positions, u_ct, centers, normals, areas, e1, e2, k=k, gamma=gamma,
+        t0=t0, dt=dt, n_samples=n_samples, c=c, split_sides=split_sides,
+        interp_bins=interp_bins, pattern=pattern, roughness=roughness,
+        taper_s=taper_s, d_phi_area=d_phi_area, block_size=block_size,
+        window_cull=window_cull, precision=precision, device=device)
+    field, dropped = plan.run()
+    return plan.to_numpy(field, dropped, out_dtype)

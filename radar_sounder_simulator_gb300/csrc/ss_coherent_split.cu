@@ -17,199 +17,24 @@
 // summed in float64 by the reduce kernel.
 #include "ss_coherent.cuh"
 #include "ss_df.cuh"
-
-#define SS_PAT_MAX 256
+#include "ss_f32.cuh"
 
 namespace ss {
 
-__constant__ float kTwoPiH = 6.28318548202514648f;     // float(2 pi)
-__constant__ float kTwoPiM = -1.74845553146951e-07f;   // 2 pi - kTwoPiH
-
-__device__ __forceinline__ float reduce_2pi(float x) {
-  const float n = rintf(x * 0.159154943091895336f);
-  float r = __fmaf_rn(-n, 6.28318548202514648f, x);
-  return __fmaf_rn(-n, -1.74845553146951e-07f, r);
-}
-
-__device__ __forceinline__ float sin_red(float x) {
-  return __sinf(reduce_2pi(x));
-}
-
-__device__ __forceinline__ float cos_red(float x) {
-  return __cosf(reduce_2pi(x));
-}
-
-// sin(x)/x
-__device__ __forceinline__ float sinc32(float x) {
-  if (fabsf(x) < 1e-4f) return 1.0f - x * x * (1.0f / 6.0f);
-  return __fdividef(sin_red(x), x);
-}
-
-__device__ __forceinline__ float dot3f(float ax, float ay, float az, float bx,
-                                       float by, float bz) {
-  return __fmaf_rn(az, bz, __fmaf_rn(ay, by, ax * bx));
-}
-
-__device__ __forceinline__ float element_field32(float cb, float q,
-                                                 float enabled) {
-  if (enabled == 0.0f) return 1.0f;
-  if (!(cb >= 0.0f)) return 0.0f;
-  float c = fminf(fmaxf(cb, 0.0f), 1.0f);
-  return c > 0.0f ? __powf(c, 0.5f * q) : (q == 0.0f ? 1.0f : 0.0f);
-}
-
-// float32 twin of gain64 (antenna.py:204-258); pa then pb staged in `tab`.
-__device__ __forceinline__ float gain32(int kind, int n, int pa_len,
-                                        const float *tab, const float *pv,
-                                        float dx, float dy, float dz) {
-  const float *pa = tab, *pb = tab + pa_len;
-  switch (kind) {
-    case SS_PAT_DIPOLE: {
-      float ca = dot3f(dx, dy, dz, pv[0], pv[1], pv[2]);
-      float s = sqrtf(fmaxf(1.0f - ca * ca, 1e-12f));
-      return __fdividef(__cosf(1.57079632679f * ca), s);
-    }
-    case SS_PAT_ARRAY: {
-      float ne = pa[0];
-      float u = dot3f(dx, dy, dz, pv[0], pv[1], pv[2]);
-      float ct = dot3f(dx, dy, dz, pv[3], pv[4], pv[5]);
-      float x = 3.14159265359f * pb[0] * u;
-      float sx = sin_red(x);
-      float af = fabsf(sx) < 1e-5f ? __fdividef(cos_red(ne * x), cos_red(x))
-                                   : __fdividef(sin_red(ne * x), ne * sx);
-      return pb[1] * element_field32(ct, pb[2], pb[3]) * fabsf(af);
-    }
-    case SS_PAT_ARRAY_TAPERED: {
-      float u = dot3f(dx, dy, dz, pv[0], pv[1], pv[2]);
-      float ct = dot3f(dx, dy, dz, pv[3], pv[4], pv[5]);
-      float ctx = 0, stx = 0, crx = 0, srx = 0, wt = 0, wr = 0;
-      for (int j = 0; j < n; ++j) {
-        float mj = (float)j - 0.5f * (float)(n - 1);
-        float ph = reduce_2pi(6.28318530718f * pb[0] * u * mj);
-        float s, c;
-        __sincosf(ph, &s, &c);
-        ctx += pa[j] * c;
-        stx += pa[j] * s;
-        crx += pa[n + j] * c;
-        srx += pa[n + j] * s;
-        wt += pa[j];
-        wr += pa[n + j];
-      }
-      float aft = sqrtf(ctx * ctx + stx * stx) / wt;
-      float afr = sqrtf(crx * crx + srx * srx) / wr;
-      return pb[1] * element_field32(ct, pb[2], pb[3]) * sqrtf(aft * afr);
-    }
-    case SS_PAT_FINITE_DIPOLE: {
-      float kh = 3.14159265359f * pa[0];
-      float ca = dot3f(dx, dy, dz, pv[0], pv[1], pv[2]);
-      float s = sqrtf(fmaxf(1.0f - ca * ca, 1e-12f));
-      float ck = __cosf(kh);
-      return __fdividef(fabsf(__cosf(kh * ca) - ck), s * (1.0f - ck));
-    }
-    case SS_PAT_TABULATED: {
-      float ct = fminf(fmaxf(dot3f(dx, dy, dz, pv[0], pv[1], pv[2]), -1.0f),
-                       1.0f);
-      float th = acosf(ct);
-      if (th <= pa[0]) return pb[0];
-      if (th >= pa[n - 1]) return pb[n - 1];
-      int lo = 0, hi = n - 1;
-      while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (pa[mid] <= th) lo = mid; else hi = mid;
-      }
-      float slope = (pb[hi] - pb[lo]) / (pa[hi] - pa[lo]);
-      return __fmaf_rn(slope, th - pa[lo], pb[lo]);
-    }
-    default:
-      return 1.0f;
-  }
-}
-
-// Weideman w(z) in float32 (roughness.py:67-80).
-__device__ __forceinline__ void faddeeva32(const float *a, float L, float zr,
-                                           float zi, float &wr, float &wi) {
-  float dr = L + zi, di = -zr;
-  float nr = L - zi, ni = zr;
-  float inv = __fdividef(1.0f, dr * dr + di * di);
-  float Zr = (nr * dr + ni * di) * inv;
-  float Zi = (ni * dr - nr * di) * inv;
-  float pr = a[0], pi = 0.0f;
-#pragma unroll 8
-  for (int j = 1; j < SS_FAD_N; ++j) {
-    float tr = __fmaf_rn(pr, Zr, __fmaf_rn(-pi, Zi, a[j]));
-    pi = __fmaf_rn(pr, Zi, pi * Zr);
-    pr = tr;
-  }
-  float ir = dr * inv, ii = -di * inv;
-  float i2r = ir * ir - ii * ii, i2i = 2.0f * ir * ii;
-  wr = 2.0f * (pr * i2r - pi * i2i) + 0.564189583548f * ir;
-  wi = 2.0f * (pr * i2i + pi * i2r) + 0.564189583548f * ii;
-}
-
-__device__ __forceinline__ float f_factor32(const float *fa, float L, float m,
-                                            float a0, float edge, float l) {
-  float sq = sqrtf(m);
-  float x = a0 * l / (2.0f * sq);
-  float y = edge * sq / l;
-  float ex2 = __expf(-x * x), ey2 = __expf(-y * y);
-  float wzr, wzi, wxr, wxi;
-  faddeeva32(fa, L, x, y, wzr, wzi);
-  faddeeva32(fa, L, x, 0.0f, wxr, wxi);
-  float ae = reduce_2pi(a0 * edge);
-  float sr, cr;
-  __sincosf(ae, &sr, &cr);
-  float ar_ = x * cr - y * sr, ai_ = x * sr + y * cr;
-  float qi = ar_ * wzi + ai_ * wzr;
-  float t1 = -y * ex2 + ey2 * qi;
-  float t2 = x * wxi;
-  return 1.0f - ey2 * cr + 1.77245385091f * (t1 - t2);
-}
-
-// D_Phi in float32; lg[m] = lgamma(m + 1).
-template <int KIND>
-__device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
-                                         const float *fa, float fL,
-                                         float sigma, float l, float K,
-                                         float A0, float B0, float Lx,
-                                         float Ly) {
-  const float sk = sigma * K;
-  const float x = sk * sk;
-  if (!(x > 0.0f)) return 0.0f;
-  const float logx = __logf(x);
-  const float kb2 = A0 * A0 + B0 * B0;
-  float acc = 0.0f;
-  if (KIND == SS_ROUGH_GAUSS_AREA) {
-    const float c = 0.25f * kb2 * l * l;
-    const float pref = 3.14159265359f * l * l * Lx * Ly;
-    for (int m = 1; m <= n_terms; ++m) {
-      const float mf = (float)m;
-      const float im = __fdividef(1.0f, mf);
-      const float e = __fmaf_rn(mf, logx, -lg[m]) - x - c * im;
-      acc = __fmaf_rn(__expf(e), pref * im, acc);
-    }
-  } else if (KIND == SS_ROUGH_EXP_AREA) {
-    const float pref = 6.28318530718f * l * l * Lx * Ly;
-    const float kl2 = kb2 * l * l;
-    for (int m = 1; m <= n_terms; ++m) {
-      const float mf = (float)m;
-      const float im = __fdividef(1.0f, mf);
-      const float im2 = im * im;
-      const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
-      const float rs = rsqrtf(__fmaf_rn(kl2, im2, 1.0f));
-      acc = __fmaf_rn(__expf(e), pref * im2 * rs * rs * rs, acc);
-    }
-  } else {
-    const float l4 = (l * l) * (l * l);
-    for (int m = 1; m <= n_terms; ++m) {
-      const float mf = (float)m;
-      const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
-      const float w = __expf(e);
-      if (w == 0.0f) continue;
-      acc += w * (l4 / (mf * mf)) * f_factor32(fa, fL, mf, A0, Lx, l) *
-             f_factor32(fa, fL, mf, B0, Ly, l);
-    }
-  }
-  return fmaxf(acc, 0.0f);
+// (dh + dl) . e for a double-float vector d and float e: exact products
+// (two_prod), compensated sum, rounded once to float.
+__device__ __forceinline__ float dot_df(float xh, float xl, float yh, float yl,
+                                        float zh, float zl, float ex, float ey,
+                                        float ez) {
+  float px, qx, py, qy, pz, qz, s, e1, e2;
+  two_prod(xh, ex, px, qx);
+  two_prod(yh, ey, py, qy);
+  two_prod(zh, ez, pz, qz);
+  two_sum(px, py, s, e1);
+  two_sum(s, pz, s, e2);
+  const float lo = (e1 + e2) + (qx + qy + qz) +
+                   __fmaf_rn(xl, ex, __fmaf_rn(yl, ey, zl * ez));
+  return s + lo;
 }
 
 struct SplitConsts {
@@ -341,8 +166,13 @@ coherent_split_kernel(CoArgs a, SplitConsts k) {
       // --- amplitude (float32) ---
       const float rx = dxh * inv_r, ry = dyh * inv_r, rz = dzh * inv_r;
       const float cosv = dot3f(rx, ry, rz, nx, ny, nz);
-      const float d1 = dot3f(rx, ry, rz, e1x, e1y, e1z);
-      const float d2 = dot3f(rx, ry, rz, e2x, e2y, e2z);
+      // r_hat . e: the sinc argument k (r_hat . e) reaches tens of radians,
+      // and its products cancel to ~1e-2 of their size near nadir, so the
+      // dot product is formed error-free (two_prod) from the double-float d
+      const float d1 = dot_df(dxh, dxl, dyh, dyl, dzh, dzl, e1x, e1y, e1z) *
+                       inv_r;
+      const float d2 = dot_df(dxh, dxl, dyh, dyl, dzh, dzl, e2x, e2y, e2z) *
+                       inv_r;
       const float inv_r2 = inv_r * inv_r;
       float amp = k.amp_pref * gam * cosv * area * sinc32(k.k * d1) *
                   sinc32(k.k * d2) * inv_r2;

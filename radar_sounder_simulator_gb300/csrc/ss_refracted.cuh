@@ -11,7 +11,7 @@ struct RefArgs {
   const int32_t *off;
   int T, N, pv_len;
   // crossed stack (top-down, joint pads first)
-  int ni, k_pad;
+  int ni, k_pad, leg_last;  // final leg uses leg index leg_last
   ss_interface ifc[SS_MAX_IFACE];
   double n_leg[SS_MAX_IFACE + 1], eps_leg[SS_MAX_IFACE + 1],
       att_leg[SS_MAX_IFACE + 1], sig_c[SS_MAX_IFACE];

@@ -120,7 +120,7 @@ def config1(seed=1):
 
 
 def config2(seed=2, n_cells=512, n_traces=1024, spacing=50.0,
-            trace_spacing=25.0):
+            trace_spacing=25.0, line_offset_y=0.0):
     """Multilayer with refraction: surface + horizons at 300 m and 1200 m +
     bed at 2500 m, each n_cells^2 facets of ``spacing`` metres; 1024 traces
     at 20 km; 60 MHz / 15 MHz.
@@ -130,13 +130,15 @@ def config2(seed=2, n_cells=512, n_traces=1024, spacing=50.0,
     5 km; relative permittivity contrast 1e-3 at both horizons (their target
     reflection coefficient fresnel_normal(eps, eps (1 + 1e-3))); firn column
     above the first horizon as one medium of delay-equivalent index; 25 m
-    trace spacing; bed reflectivity +10^(R/20) with R ~ U[-30, -5] dB."""
+    trace spacing; bed reflectivity +10^(R/20) with R ~ U[-30, -5] dB.
+    ``line_offset_y`` shifts the track cross-track (one line per GPU)."""
     rng = np.random.default_rng(seed)
     surf = surface(n_cells, spacing, 20.0, 5000.0, 0.0, rng)
     h1 = surface(n_cells, spacing, 5.0, 1000.0, -300.0, rng)
     h2 = surface(n_cells, spacing, 5.0, 1000.0, -1200.0, rng)
     bed = surface(n_cells, spacing, 300.0, 5000.0, -2500.0, rng)
     pos, uct = straight_track(n_traces, trace_spacing, 20000.0)
+    pos[:, 1] += line_offset_y
     n_firn = firn_n_eff(300.0)
     eps_ice = 3.15
     eps = [1.0, n_firn ** 2, eps_ice, eps_ice * (1.0 + 1e-3),

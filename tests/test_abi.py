@@ -29,3 +29,40 @@ def test_library_exports_header_symbols():
         assert hasattr(L, name), f"{name} declared but not exported"
     assert set(_lib.SIGNATURES) <= decl | {"ss_version", "ss_last_error"}
     assert b"sm_103a" in L.ss_version()
+
+
+def test_struct_layouts_match_header(tmp_path):
+    """ctypes mirrors of the ABI structs have the C layout (sizes and field
+    offsets), checked by compiling a probe against the header with gcc."""
+    import ctypes as C
+    import shutil
+    import subprocess
+    import pytest
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    structs = {"ss_facets": _lib.Facets, "ss_traces": _lib.Traces,
+               "ss_pattern": _lib.Pattern, "ss_roughness": _lib.Roughness,
+               "ss_coherent_opts": _lib.CoherentOpts,
+               "ss_output": _lib.Output, "ss_interface": _lib.Interface,
+               "ss_refracted_opts": _lib.RefractedOpts}
+    lines = ["#include <stdio.h>", "#include <stddef.h>",
+             '#include "soundersim_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", '
+                         f'offsetof({cname}, {fname}));')
+    lines.append("return 0; }")
+    src = tmp_path / "probe.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "probe"
+    subprocess.run(["gcc", f"-I{os.path.join(ROOT, 'include')}", str(src),
+                    "-o", str(exe)], check=True)
+    out = dict(line.rsplit(" ", 1) for line in
+               subprocess.run([str(exe)], capture_output=True, text=True,
+                              check=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(out[cname]) == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(out[f"{cname}.{fname}"]) == getattr(py, fname).offset, \
+                f"{cname}.{fname}"
