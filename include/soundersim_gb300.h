@@ -154,6 +154,40 @@ int ss_coherent_fwd(const ss_coherent_opts *opts, const ss_facets *facets,
                     const ss_roughness *rough, const ss_output *out,
                     void *scratch, size_t scratch_bytes, void *stream);
 
+/* ---- surface facet sum without caller scratch ------------------------ */
+
+/* Size of the fixed device scratch array behind ss_coherent_fwd_noalloc. */
+#define SS_NOALLOC_SCRATCH_BYTES (64u << 20)
+
+/* ss_coherent_fwd for callers that cannot allocate device memory: the same
+ * inputs, outputs and results (within float rounding: it may sum the facet
+ * chunks in fewer groups), with the scratch taken from a fixed array of
+ * SS_NOALLOC_SCRATCH_BYTES compiled into this library instead of a caller
+ * buffer. It has no counterpart in the reference, which only runs inside
+ * its own Python process and leaves device memory to XLA.
+ *
+ * Who needs it: programs whose device memory belongs to another allocator
+ * (a framework's pool, or a budget fixed at start-up) and processing loops
+ * that must not allocate once running, so they cannot hand ss_coherent_fwd
+ * a scratch buffer.
+ *
+ * Limits and sharing: one facet chunk of partial histograms for all traces,
+ * n_traces * n_samples * (2 with split_sides) * (16 bytes FP64, 8 bytes
+ * split) + 8 bytes per trace, must fit in the array, else SS_ERR_SCRATCH
+ * is returned before any work is queued. The array is reserved on every GPU
+ * that loads the library until the process exits. The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that call before any stream capture. All calls
+ * share the array and leave their partials in it: calls that overlap on the
+ * GPU (different streams or host threads) race. Nothing in it needs
+ * clearing, since every partial read is first written by the same call.
+ * No device memory is allocated or freed. */
+int ss_coherent_fwd_noalloc(const ss_coherent_opts *opts,
+                            const ss_facets *facets, const ss_traces *traces,
+                            const ss_pattern *pattern,
+                            const ss_roughness *rough, const ss_output *out,
+                            void *stream);
+
 /* ---- refracted multilayer facet sum ---------------------------------- */
 
 #define SS_MAX_IFACE 8  /* crossed interfaces per call (after padding) */

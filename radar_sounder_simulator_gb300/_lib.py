@@ -90,6 +90,11 @@ SIGNATURES = {
                                   C.POINTER(Traces), C.POINTER(Pattern),
                                   C.POINTER(Roughness), C.POINTER(Output),
                                   C.c_void_p, C.c_size_t, C.c_void_p]),
+    "ss_coherent_fwd_noalloc": (C.c_int, [C.POINTER(CoherentOpts),
+                                          C.POINTER(Facets), C.POINTER(Traces),
+                                          C.POINTER(Pattern),
+                                          C.POINTER(Roughness),
+                                          C.POINTER(Output), C.c_void_p]),
     "ss_refracted_scratch_bytes": (C.c_size_t, [C.POINTER(RefractedOpts),
                                                 C.c_int32, C.c_int32]),
     "ss_refracted_fwd": (C.c_int, [C.POINTER(RefractedOpts),
