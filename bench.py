@@ -40,7 +40,13 @@ def parse():
     ap.add_argument("--n-cells", type=int, default=512)
     ap.add_argument("--n-traces", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--skip-fp64", action="store_true")
+    ap.add_argument("--skip-fp64", action="store_true",
+                    help="skip the float64-form step and the error check")
+    ap.add_argument("--skip-e2e", action="store_true",
+                    help="skip the drop-in (host buffers) step")
+    ap.add_argument("--fp64-traces", type=int, default=256,
+                    help="traces of the float64-form step (its rate is per "
+                         "pair; the error check covers these traces)")
     return ap.parse_args()
 
 
@@ -329,11 +335,19 @@ def main():
                                  for s in range(args.steps)]))
                   for i in range(len(plans))]
 
-    # float64 form on the same scene (one step) and the split form's error
+    # float64 form on the first traces of the same scene (one step) and the
+    # split form's error on those traces
     fp64 = None
     err = None
     if not args.skip_fp64:
-        plans64 = build_plans(cfg, "fp64", device)
+        sub = scenes.config2(n_cells=args.n_cells, n_traces=args.n_traces,
+                             line_offset_y=200.0 * rank)
+        nt = min(args.fp64_traces, args.n_traces)
+        sub.pos, sub.uct = cfg.pos[:nt], cfg.uct[:nt]
+        sub.t0 = cfg.t0
+        plans64 = build_plans(sub, "fp64", device)
+        plans32 = build_plans(sub, "split", device)
+        outs32 = [p.run() for p in plans32]
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -343,24 +357,28 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         ms64 = e0.elapsed_time(e1)
-        fp64 = {"value": pairs_step / (ms64 * 1e-3), "unit": UNIT,
-                "ms_per_step": ms64}
-        err = split_error(outs, outs64)
-        del plans64, outs64
+        pairs64 = sum(len(f.centers) for f in sub.layers) * nt
+        fp64 = {"value": pairs64 / (ms64 * 1e-3), "unit": UNIT,
+                "ms_per_step": ms64 * len(cfg.pos) / nt,
+                "traces_timed": nt}
+        err = split_error(outs32, outs64)
+        del plans64, outs64, plans32, outs32
 
     # end to end through the drop-in API with host buffers
     h2d, d2h = host_bytes(cfg)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    drop_in_step(cfg, "split", device)
-    torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = None
+    if not args.skip_e2e:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        drop_in_step(cfg, "split", device)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
 
     launches = args.steps * sum(coherent_run_count(p) for p in plans)
     roof = roofline(per_kernel, plans)
     if rank == 0:
         cpu = None
-        if ws == 1:
+        if ws == 1 and args.cpu_seconds > 0:
             v, sample = cpu_sample_rate(cfg, args.cpu_seconds,
                                         os.cpu_count() or 1)
             cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1,
@@ -371,9 +389,9 @@ def main():
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
                 "data": "synthetic (seeded config-2 scene)",
                 "config": config_dict(args, ws),
-                "e2e": {"value": pairs_step / e2e_s, "unit": UNIT,
-                        "h2d_bytes_per_step": h2d,
-                        "d2h_bytes_per_step": d2h},
+                "e2e": ({"value": pairs_step / e2e_s, "unit": UNIT,
+                         "h2d_bytes_per_step": h2d,
+                         "d2h_bytes_per_step": d2h} if e2e_s else None),
                 "fp64": fp64,
                 "split_over_fp64": (value / ws / fp64["value"]) if fp64
                 else None,

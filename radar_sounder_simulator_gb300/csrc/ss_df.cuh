@@ -45,4 +45,66 @@ __host__ __device__ __forceinline__ df df_from_double(double v) {
   return r;
 }
 
+__device__ __forceinline__ df df_make(float hi, float lo) {
+  df r;
+  fast_two_sum(hi, lo, r.hi, r.lo);
+  return r;
+}
+
+// a - b of two floats, exactly.
+__device__ __forceinline__ df df_diff(float a, float b) {
+  df r;
+  two_sum(a, -b, r.hi, r.lo);
+  return r;
+}
+
+__device__ __forceinline__ df df_add_f(df a, float b) {
+  float s, e;
+  two_sum(a.hi, b, s, e);
+  return df_make(s, e + a.lo);
+}
+
+__device__ __forceinline__ df df_add(df a, df b) {
+  float s, e;
+  two_sum(a.hi, b.hi, s, e);
+  return df_make(s, e + (a.lo + b.lo));
+}
+
+__device__ __forceinline__ df df_mul_f(df a, float b) {
+  float p, e;
+  two_prod(a.hi, b, p, e);
+  return df_make(p, __fmaf_rn(a.lo, b, e));
+}
+
+__device__ __forceinline__ df df_mul(df a, df b) {
+  float p, e;
+  two_prod(a.hi, b.hi, p, e);
+  e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+  return df_make(p, e);
+}
+
+// |v| of a double-float 3-vector: sum of exact squares, then an rsqrt seed
+// with one Newton correction (relative error ~1e-14).
+__device__ __forceinline__ df df_norm3(df x, df y, df z) {
+  float qx, ex, qy, ey, qz, ez;
+  two_prod(x.hi, x.hi, qx, ex);
+  two_prod(y.hi, y.hi, qy, ey);
+  two_prod(z.hi, z.hi, qz, ez);
+  float s1, e1, sh, e2;
+  two_sum(qx, qy, s1, e1);
+  two_sum(s1, qz, sh, e2);
+  float sl = (e1 + e2) + (ex + ey + ez) +
+             2.0f * (x.hi * x.lo + y.hi * y.lo + z.hi * z.lo);
+  fast_two_sum(sh, sl, sh, sl);
+  if (!(sh > 0.0f)) return df_make(0.0f, 0.0f);
+  const float r = rsqrtf(sh);
+  const float r0 = sh * r;
+  const float res = __fmaf_rn(-r0, r0, sh) + sl;
+  return df_make(r0, res * (0.5f * r));
+}
+
+__host__ __device__ __forceinline__ double df_to_double(df a) {
+  return (double)a.hi + (double)a.lo;
+}
+
 }  // namespace ss

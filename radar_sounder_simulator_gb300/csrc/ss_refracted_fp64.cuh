@@ -22,7 +22,7 @@ __device__ __forceinline__ double dot3v(const double *a, const double *b) {
 
 // Two-point crossing (refraction.py:78-161; `comp` selects the component
 // form of multilayer.py:196-266).
-static __device__ void snell64(const double *p, const double *q, const double *o,
+static __device__ __noinline__ void snell64(const double *p, const double *q, const double *o,
                         const double *nrm, double n1, double n2, int n_iter,
                         bool comp, Snell64 &R) {
   double po[3] = {p[0] - o[0], p[1] - o[1], p[2] - o[2]};
@@ -155,7 +155,7 @@ __device__ __forceinline__ void inv2x2(const double (&m)[2][2],
 }
 
 template <int NI>
-static __device__ void joint64(const double *p, const double *q,
+static __device__ __noinline__ void joint64(const double *p, const double *q,
                         const double (&O)[NI][3], const double (&Nn)[NI][3],
                         const double *nm, int n_newton, int n_backtrack,
                         double (&X)[NI][3], double (&th1)[NI],
@@ -339,7 +339,7 @@ struct Path64 {
   double opl, loss_db, sum_par, sum_perp, tau2, c0, c_last;
 };
 
-static __device__ void path_sequential64(const RefArgs &a, const double *p,
+static __device__ __noinline__ void path_sequential64(const RefArgs &a, const double *p,
                                   const double *q, Path64 &P) {
   double cur[3] = {p[0], p[1], p[2]};
   P.valid = true;
@@ -381,7 +381,7 @@ static __device__ void path_sequential64(const RefArgs &a, const double *p,
 }
 
 template <int NI>
-static __device__ void path_joint64(const RefArgs &a, const double *p,
+static __device__ __noinline__ void path_joint64(const RefArgs &a, const double *p,
                              const double *q, Path64 &P) {
   // pass 1: mean-plane chain (10 iterations) anchors the lookups
   double pt[NI][3], nr[NI][3];
@@ -442,7 +442,7 @@ static __device__ void path_joint64(const RefArgs &a, const double *p,
 // validity for one pair: the exact reference quantity the split kernel falls
 // back to when a pair sits within the bin-edge guard band.
 template <int NI>
-static __device__ double full_opl64(const RefArgs &a, const double *p,
+static __device__ __noinline__ double full_opl64(const RefArgs &a, const double *p,
                                     const double *q, bool &valid) {
   Path64 P;
   if (NI == 0)

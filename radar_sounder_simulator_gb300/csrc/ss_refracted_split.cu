@@ -1,34 +1,34 @@
 // Split-precision refracted multilayer kernel.
 //
-// The float64 form spends nearly all its time in fixed-budget Newton
-// iterations (10 + 25 per crossing, or the joint solve's 6 damped steps of
-// block-Thomas plus step halving), on GB300 whose FP64 rate is a small
-// fraction of its FP32 rate. This form keeps float64 only where the result
-// needs it and runs the iterations in float32:
+// On GB300 the FP64 pipe runs at a small fraction of the FP32 rate, and the
+// float64 form of this kernel is bound by it: fixed-budget Newton solves on
+// 20 km geometry. This form runs every solve in float32 and carries the few
+// quantities that need more than 24 bits as double-floats (hi + lo float
+// pairs on the FP32 pipe):
 //
-//   * facet lookups: the mean-plane crossing is solved in float32 in
-//     plane-relative coordinates; if the affine cell coordinate lies within
-//     1e-3 cells of a rounding boundary (the float32 crossing error is
-//     ~4e-5 cells) the float64 mean-plane solve of the reference is re-run
-//     for that pair, so lookups are the reference's integer decisions;
-//   * the local-plane two-point solve: float64 geometry (heights, feet,
-//     scale) around float32 Newton iterations; the crossing offset t comes
-//     from the float32 root and the path lengths are evaluated in float64 at
-//     that t -- the optical path is stationary in t (Fermat), so the float32
-//     root error enters only at second order;
-//   * the joint solve: float32 damped Newton on in-plane offsets measured
-//     from each local plane's facet centre (segments are formed from float64
-//     centre differences, so float32 keeps ~1e-7 of each segment), then
-//     float64 segment lengths; again second order in the root error;
-//   * optical path, carrier phase reduction and fast-time bin in float64; a
-//     pair within 1e-6 of a bin edge is re-evaluated with the complete
-//     float64 path, so bins equal the float64 form's;
-//   * everything radiometric (Fresnel, spreading, attenuation, antenna gain,
-//     sinc at k_j, roughness series, diffuse channel) in float32.
+//   * geometry relative to the local facet centres. Each two-point and joint
+//     solve is posed in coordinates measured from the plane points (mean
+//     point for the lookup pass, local facet centre for the crossing), with
+//     the long platform offset p - o formed exactly as a double-float and
+//     rounded once. The crossing is rebuilt from the short side of the ray
+//     (the target's foot for a downward ray), so the float32 root places the
+//     crossing to micrometres, which keeps the facet's arrival direction --
+//     and the sinc arguments k_j (r_hat . e) -- accurate to ~1e-8 rad;
+//   * facet lookups: the float32 mean-plane crossing gives the affine cell
+//     coordinate; if it lies within 1e-3 cells of a rounding boundary the
+//     float64 mean-plane chain of the reference is re-run for that pair, so
+//     the lookups are the reference's integer decisions;
+//   * leg lengths, optical path, carrier phase (2 k0 opl mod 2 pi) and the
+//     fast-time bin in double-float. The optical path is stationary in the
+//     crossing positions (Fermat), so their float32 error enters at second
+//     order; a pair within 1e-6 of a bin edge is re-evaluated with the
+//     complete float64 path, so bins equal the float64 form's;
+//   * radiometry (Fresnel, spreading, attenuation, antenna gain, sinc,
+//     roughness series, diffuse channel) in float32.
 //
-// Validity: same-side/shadow tests use the float64 heights; convergence uses
-// the float32 Snell residual with tolerance 1e-4 (the float32 floor is
-// ~1e-6; failed solves sit at O(0.1)).
+// Validity: same-side tests in float32 on plane-relative heights; Newton
+// convergence by the float32 Snell residual with tolerance 1e-4 (the float32
+// floor is ~1e-6; failed solves sit at O(0.1)).
 #include "ss_df.cuh"
 #include "ss_f32.cuh"
 #include "ss_refracted_fp64.cuh"
@@ -38,13 +38,26 @@ namespace ss {
 constexpr float kTiny32 = 1e-30f;
 constexpr float kEps32 = 1.1920929e-07f;
 constexpr float kTol32 = 1e-4f;
-constexpr double kLookupGuard = 1e-3;
+constexpr float kLookupGuard = 1e-3f;
 constexpr float kBinGuard = 1e-6f;
+
+// Per-interface constants of the float32 lookup pass.
+struct MeanPlane32 {
+  float mp[3];    // mean point (rounded)
+  float mn[3];    // unit mean normal
+  float dmp[3];   // mean point of the interface above minus this one
+  float coef[4];  // affine fit: row = c0 x + c2 y + rb0, col = c1 x + c3 y + rb1
+  float rb[2];    // affine value at the mean point
+};
 
 struct RefSplitConsts {
   float k0, amp_pref_j, kj, taper_inv, sigma, corr, fadL, n_exp;
-  float n_leg[SS_MAX_IFACE + 1], eps_leg[SS_MAX_IFACE + 1],
-      att_leg[SS_MAX_IFACE + 1], sig_c[SS_MAX_IFACE];
+  float K2h, K2l;             // 2 k0 as double-float
+  float Ah, Al, Bh, Bl;       // u = opl A - B, A = 2/(c dt), B = t0/dt
+  float n_leg[SS_MAX_IFACE + 1], n_leg_lo[SS_MAX_IFACE + 1],
+      eps_leg[SS_MAX_IFACE + 1], att_leg[SS_MAX_IFACE + 1],
+      sig_c[SS_MAX_IFACE];
+  MeanPlane32 mean[SS_MAX_IFACE];
 };
 
 __device__ __forceinline__ float dot3a(const float *a, const float *b) {
@@ -52,8 +65,8 @@ __device__ __forceinline__ float dot3a(const float *a, const float *b) {
 }
 
 // float32 safeguarded Newton on sigma = sin(theta_rare) (the reference's
-// update, refraction.py:120-144), stopping early once the step is below
-// float32 resolution.
+// update, refraction.py:120-144), stopping once the step is below float32
+// resolution.
 __device__ __forceinline__ float sigma32(float ar, float bd, float Lh,
                                          float ah, float bh, float ratio,
                                          int n_iter) {
@@ -79,20 +92,28 @@ __device__ __forceinline__ float sigma32(float ar, float bd, float Lh,
   return sig;
 }
 
-// float32 two-point solve with both endpoints given relative to the plane
-// point: returns the crossing offset from the plane point.
-__device__ __forceinline__ void snell32_rel(const float *P, const float *Q,
+// Two-point solve with both end points relative to the plane point.
+struct Solve32 {
+  float y[3];    // crossing relative to the plane point
+  float c1, c2;  // cos(theta) on the p side and on the q side
+  float res;     // Snell residual (closure form, like refraction.py:155)
+  bool sides;    // end points strictly on opposite sides of the plane
+};
+
+__device__ __forceinline__ void snell_rel32(const float *P, const float *Q,
                                             const float *nrm, float n1,
-                                            float n2, int n_iter, float *y) {
+                                            float n2, int n_iter,
+                                            Solve32 &S) {
   const float h1 = dot3a(P, nrm), h2 = dot3a(Q, nrm);
   const float a = fabsf(h1), b = fabsf(h2);
-  float fp[3], w[3];
+  float fp[3], fq[3], w[3];
   for (int j = 0; j < 3; ++j) {
     fp[j] = P[j] - h1 * nrm[j];
-    w[j] = (Q[j] - h2 * nrm[j]) - fp[j];
+    fq[j] = Q[j] - h2 * nrm[j];
+    w[j] = fq[j] - fp[j];
   }
   const float L = sqrtf(dot3a(w, w));
-  const float Lm = fmaxf(L, kTiny32);
+  const float iL = 1.0f / fmaxf(L, kTiny32);
   const float s = fmaxf(a + b + L, kTiny32);
   const float inv_s = 1.0f / s;
   const float ah = a * inv_s, bh = b * inv_s, Lh = L * inv_s;
@@ -100,115 +121,79 @@ __device__ __forceinline__ void snell32_rel(const float *P, const float *Q,
   const float ratio = fminf(n1, n2) / fmaxf(n1, n2);
   const float ar = swap ? bh : ah, bd = swap ? ah : bh;
   const float sig = sigma32(ar, bd, Lh, ah, bh, ratio, n_iter);
-  const float c1 = fmaxf((1.0f - sig) * (1.0f + sig), kTiny32);
-  const float tr = ar * sig * rsqrtf(c1);
-  const float t = fminf(fmaxf(swap ? Lh - tr : tr, 0.0f), Lh);
-  const float st = s * t / Lm;
-  for (int j = 0; j < 3; ++j) y[j] = fp[j] + st * w[j];
+  const float v = ratio * sig;
+  const float tr = ar * sig * rsqrtf(fmaxf((1.0f - sig) * (1.0f + sig),
+                                           kTiny32));
+  const float td = bd * v * rsqrtf(fmaxf((1.0f - v) * (1.0f + v), kTiny32));
+  // offsets from the feet of p and q along w (t_p + t_q = Lh at the root)
+  const float tp = fminf(fmaxf(swap ? td : tr, 0.0f), Lh);
+  const float tq = fminf(fmaxf(swap ? tr : td, 0.0f), Lh);
+  if (tq <= tp) {
+    const float st = s * tq * iL;
+    for (int j = 0; j < 3; ++j) S.y[j] = fq[j] - st * w[j];
+  } else {
+    const float st = s * tp * iL;
+    for (int j = 0; j < 3; ++j) S.y[j] = fp[j] + st * w[j];
+  }
+  // back onto the plane: the foot of a 20 km distant point is off the plane
+  // by (1 - |n|^2) x 20 km, and an off-plane crossing is a first-order
+  // optical-path error (in-plane errors are second order)
+  const float yn = dot3a(S.y, nrm);
+  for (int j = 0; j < 3; ++j) S.y[j] -= yn * nrm[j];
+  const float r1 = sqrtf(ah * ah + tp * tp), r2 = sqrtf(bh * bh + tq * tq);
+  S.c1 = ah / fmaxf(r1, kTiny32);
+  S.c2 = bh / fmaxf(r2, kTiny32);
+  const float d2 = Lh - tp;
+  S.res = n1 * tp / fmaxf(r1, kTiny32) -
+          n2 * d2 / fmaxf(sqrtf(bh * bh + d2 * d2), kTiny32);
+  S.sides = h1 * h2 < 0.0f;
 }
 
-// Local-plane two-point solve: float64 heights/feet/scale, float32 root,
-// float64 crossing and leg lengths at that root.
-struct LocalSolve {
-  double x[3];       // crossing (float64)
-  double s1;         // |cur - x|
-  double s2;         // |x - q|
-  float c1, c2;      // cos(theta1), cos(theta2)
-  bool valid;
-};
-
-__device__ __forceinline__ void snell_local(const double *cur, const double *q,
-                                            const double *o, const double *nrm,
-                                            double n1, double n2, int n_iter,
-                                            LocalSolve &R) {
-  double po[3] = {cur[0] - o[0], cur[1] - o[1], cur[2] - o[2]};
-  double qo[3] = {q[0] - o[0], q[1] - o[1], q[2] - o[2]};
-  const double h1 = dot3v(po, nrm), h2 = dot3v(qo, nrm);
-  const double a = fabs(h1), b = fabs(h2);
-  double fp[3], w[3];
-  for (int j = 0; j < 3; ++j) {
-    fp[j] = cur[j] - h1 * nrm[j];
-    w[j] = (q[j] - h2 * nrm[j]) - fp[j];
-  }
-  const double L = sqrt(dot3v(w, w));
-  const double s = fmax(a + b + L, kTiny);
-  const double inv_s = 1.0 / s;
-  const double ah = a * inv_s, bh = b * inv_s, Lh = L * inv_s;
-  const bool swap = n1 > n2;
-  const float ratio = (float)(fmin(n1, n2) / fmax(n1, n2));
-  const float ah32 = (float)ah, bh32 = (float)bh, Lh32 = (float)Lh;
-  const float ar32 = swap ? bh32 : ah32, bd32 = swap ? ah32 : bh32;
-  const float sig32 = sigma32(ar32, bd32, Lh32, ah32, bh32, ratio, n_iter);
-  // one float64 Newton step from the float32 root: the crossing enters the
-  // facet's arrival direction (and so the sinc arguments) at first order
-  const double ar = swap ? bh : ah, bd = swap ? ah : bh;
-  const double ratio64 = fmin(n1, n2) / fmax(n1, n2);
-  double sg = (double)sig32;
-  {
-    const double v = ratio64 * sg;
-    const double r1i = rsqrt(fmax((1.0 - sg) * (1.0 + sg), kTiny));
-    const double r2i = rsqrt(fmax((1.0 - v) * (1.0 + v), kTiny));
-    const double F = (ar * sg * r1i + bd * v * r2i) - Lh;
-    const double Fp = ar * r1i * r1i * r1i + bd * ratio64 * r2i * r2i * r2i;
-    const double sn = sg - F / fmax(Fp, kTiny);
-    if (isfinite(sn) && sn >= 0.0 && sn < 1.0) sg = sn;
-  }
-  const double tr = ar * sg * rsqrt(fmax((1.0 - sg) * (1.0 + sg), kTiny));
-  const double t = fmin(fmax(swap ? Lh - tr : tr, 0.0), Lh);
-  const double d2 = Lh - t;
-  const double r1 = fmax(sqrt(ah * ah + t * t), kTiny);
-  const double r2 = fmax(sqrt(bh * bh + d2 * d2), kTiny);
-  R.s1 = s * r1;
-  R.s2 = s * r2;
-  const double stl = s * t / fmax(L, kTiny);
-  for (int j = 0; j < 3; ++j) R.x[j] = fp[j] + stl * w[j];
-  R.c1 = (float)(ah / r1);
-  R.c2 = (float)(bh / r2);
-  const float res = (float)n1 * (float)(t / r1) - (float)n2 * (float)(d2 / r2);
-  R.valid = (h1 * h2 < 0.0) && (fabsf(res) <= kTol32);
+// Affine cell of a float32 mean-plane crossing (offset y from the mean
+// point); false when either coordinate is within the guard band of a
+// rounding boundary.
+__device__ __forceinline__ bool cell_of(const MeanPlane32 &M,
+                                        const ss_interface &I, const float *y,
+                                        int &row, int &col) {
+  const float rc0 = M.rb[0] + (y[0] * M.coef[0] + y[1] * M.coef[2]);
+  const float rc1 = M.rb[1] + (y[0] * M.coef[1] + y[1] * M.coef[3]);
+  const float f0 = rc0 - floorf(rc0), f1 = rc1 - floorf(rc1);
+  row = (int)fminf(fmaxf(rintf(rc0), 0.0f), (float)(I.ny - 1));
+  col = (int)fminf(fmaxf(rintf(rc1), 0.0f), (float)(I.nx - 1));
+  return fabsf(f0 - 0.5f) > kLookupGuard && fabsf(f1 - 0.5f) > kLookupGuard;
 }
 
-// Mean-plane crossing in float32 relative to the mean point, then the
-// affine cell coordinate; returns false when either coordinate is within
-// the guard band of a rounding boundary.
-__device__ __forceinline__ bool mean_lookup32(const ss_interface &I,
-                                              const double *cur,
-                                              const double *q, float n1,
-                                              float n2, int n_iter, int &row,
-                                              int &col) {
-  const float P[3] = {(float)(cur[0] - I.mean_point[0]),
-                      (float)(cur[1] - I.mean_point[1]),
-                      (float)(cur[2] - I.mean_point[2])};
-  const float Q[3] = {(float)(q[0] - I.mean_point[0]),
-                      (float)(q[1] - I.mean_point[1]),
-                      (float)(q[2] - I.mean_point[2])};
-  const float nrm[3] = {(float)I.mean_normal[0], (float)I.mean_normal[1],
-                        (float)I.mean_normal[2]};
-  float y[3];
-  snell32_rel(P, Q, nrm, n1, n2, n_iter, y);
-  const double b0 = I.mean_point[0] * I.coef[0] + I.mean_point[1] * I.coef[2] +
-                    I.coef[4];
-  const double b1 = I.mean_point[0] * I.coef[1] + I.mean_point[1] * I.coef[3] +
-                    I.coef[5];
-  const double rc0 = b0 + (double)(y[0] * (float)I.coef[0] +
-                                   y[1] * (float)I.coef[2]);
-  const double rc1 = b1 + (double)(y[0] * (float)I.coef[1] +
-                                   y[1] * (float)I.coef[3]);
-  const double f0 = rc0 - floor(rc0), f1 = rc1 - floor(rc1);
-  const bool safe = fabs(f0 - 0.5) > kLookupGuard &&
-                    fabs(f1 - 0.5) > kLookupGuard;
+// Exact reference cell from a float64 mean-plane solve (multilayer.py
+// :375-381 for comp = true, refraction_joint sequential chain for false).
+__device__ __noinline__ void cell64(const ss_interface &I, const double *cur,
+                                    const double *q, double n1, double n2,
+                                    bool comp, double *x_out, int &row,
+                                    int &col) {
+  Snell64 R;
+  snell64(cur, q, I.mean_point, I.mean_normal, n1, n2, 10, comp, R);
+  const double rc0 = __dadd_rn(__dadd_rn(__dmul_rn(R.x[0], I.coef[0]),
+                                         __dmul_rn(R.x[1], I.coef[2])),
+                               I.coef[4]);
+  const double rc1 = __dadd_rn(__dadd_rn(__dmul_rn(R.x[0], I.coef[1]),
+                                         __dmul_rn(R.x[1], I.coef[3])),
+                               I.coef[5]);
   row = (int)fmin(fmax(rint(rc0), 0.0), (double)(I.ny - 1));
   col = (int)fmin(fmax(rint(rc1), 0.0), (double)(I.nx - 1));
-  return safe;
+  for (int j = 0; j < 3; ++j) x_out[j] = R.x[j];
 }
 
-__device__ __forceinline__ void cell_plane(const ss_interface &I, int row,
-                                           int col, double *pt, double *nr) {
+__device__ __forceinline__ void cell_plane32(const ss_interface &I, int row,
+                                             int col, float *o, float *n) {
   const float *g = I.table + ((size_t)row * I.nx + col) * 6;
   for (int j = 0; j < 3; ++j) {
-    pt[j] = (double)g[j];
-    nr[j] = (double)g[3 + j];
+    o[j] = g[j];
+    n[j] = g[3 + j];
   }
+  // unit length to float32 rounding (rsqrt seed + one Newton step)
+  const float nn = dot3a(n, n);
+  float in = rsqrtf(nn);
+  in = in * __fmaf_rn(-0.5f * nn * in, in, 1.5f);
+  for (int j = 0; j < 3; ++j) n[j] *= in;
 }
 
 __device__ __forceinline__ float fresnel_gamma32(float e1, float e2,
@@ -219,151 +204,169 @@ __device__ __forceinline__ float fresnel_gamma32(float e1, float e2,
   return (n1 * c1 - n2 * c2) / (n1 * c1 + n2 * c2);
 }
 
+// Per-trace platform data staged in shared memory.
+struct TraceS {
+  float ph[3], pl[3];  // position as double-float
+  float pm0[3];        // p - mean point of the first interface (rounded)
+};
+
 struct PathS {
-  double cur[3], xf[3];
-  double opl;
+  df opl;              // optical path over the legs above the final one
+  df s_last;           // final-leg length
+  float rh[3];         // unit vector facet -> last crossing
+  float d0[3];         // platform -> first crossing
   float loss_db, sum_par, sum_perp, tau2, c0, c_last;
   bool valid;
 };
 
+// p - o as a double-float vector (o a float point).
+__device__ __forceinline__ void p_minus(const TraceS &T, const float *o,
+                                        df *out) {
+  for (int j = 0; j < 3; ++j) {
+    float s, e;
+    two_sum(T.ph[j], -o[j], s, e);
+    out[j] = df_make(s, e + T.pl[j]);
+  }
+}
+
+// ---------------------------------------------------------------------
+// sequential chain (multilayer.py:352-406)
+// ---------------------------------------------------------------------
 __device__ void path_sequential_split(const RefArgs &a,
                                       const RefSplitConsts &k,
-                                      const double *p, const double *q,
-                                      PathS &P) {
-  double cur[3] = {p[0], p[1], p[2]};
+                                      const TraceS &T, const double *p64,
+                                      const float *q, PathS &P) {
+  float o_prev[3] = {0, 0, 0}, y_prev[3] = {0, 0, 0};
+  df Pd[3], Qd[3];
+  float y[3] = {0, 0, 0};
   P.valid = true;
-  P.opl = 0.0;
+  P.opl = df_make(0.0f, 0.0f);
   P.loss_db = P.sum_par = P.sum_perp = 0.0f;
   P.tau2 = 1.0f;
   P.c0 = P.c_last = 1.0f;
   for (int i = 0; i < a.ni; ++i) {
     const ss_interface &I = a.ifc[i];
-    int row, col;
-    if (!mean_lookup32(I, cur, q, k.n_leg[i], k.n_leg[i + 1], 10, row,
-                       col)) {
-      Snell64 R1;  // exact reference decision near a rounding boundary
-      snell64(cur, q, I.mean_point, I.mean_normal, a.n_leg[i],
-              a.n_leg[i + 1], 10, true, R1);
-      double pt[3], nr[3];
-      lookup64(I, R1.x, pt, nr);
-      const double rc0 = __dadd_rn(__dadd_rn(__dmul_rn(R1.x[0], I.coef[0]),
-                                             __dmul_rn(R1.x[1], I.coef[2])),
-                                   I.coef[4]);
-      const double rc1 = __dadd_rn(__dadd_rn(__dmul_rn(R1.x[0], I.coef[1]),
-                                             __dmul_rn(R1.x[1], I.coef[3])),
-                                   I.coef[5]);
-      row = (int)fmin(fmax(rint(rc0), 0.0), (double)(I.ny - 1));
-      col = (int)fmin(fmax(rint(rc1), 0.0), (double)(I.nx - 1));
+    const MeanPlane32 &M = k.mean[i];
+    // facet lookup from the mean-plane crossing
+    float Pm[3], Qm[3];
+    for (int j = 0; j < 3; ++j) {
+      Pm[j] = i == 0 ? T.pm0[j] : (o_prev[j] - M.mp[j]) + y_prev[j];
+      Qm[j] = q[j] - M.mp[j];
     }
-    double pt[3], nr[3];
-    cell_plane(I, row, col, pt, nr);
-    const double inn = 1.0 / sqrt(dot3v(nr, nr));
-    for (int j = 0; j < 3; ++j) nr[j] *= inn;
-    LocalSolve R;
-    snell_local(cur, q, pt, nr, a.n_leg[i], a.n_leg[i + 1], 25, R);
-    P.valid = P.valid && R.valid;
-    const float c_inc = fmaxf(R.c1, (float)kCMin);
+    Solve32 Sm;
+    snell_rel32(Pm, Qm, M.mn, k.n_leg[i], k.n_leg[i + 1], 10, Sm);
+    int row, col;
+    if (!cell_of(M, I, Sm.y, row, col)) {
+      double cur64[3], q64[3] = {q[0], q[1], q[2]}, x1[3];
+      for (int j = 0; j < 3; ++j)
+        cur64[j] = i == 0 ? p64[j] : (double)o_prev[j] + (double)y_prev[j];
+      cell64(I, cur64, q64, a.n_leg[i], a.n_leg[i + 1], true, x1, row, col);
+    }
+    float o[3], n[3];
+    cell_plane32(I, row, col, o, n);
+    // local-plane solve relative to the facet centre o
+    if (i == 0) {
+      p_minus(T, o, Pd);
+    } else {
+      for (int j = 0; j < 3; ++j)
+        Pd[j] = df_add_f(df_diff(o_prev[j], o[j]), y_prev[j]);
+    }
+    for (int j = 0; j < 3; ++j) Qd[j] = df_diff(q[j], o[j]);
+    const float Ph[3] = {Pd[0].hi, Pd[1].hi, Pd[2].hi};
+    const float Qh[3] = {Qd[0].hi, Qd[1].hi, Qd[2].hi};
+    Solve32 S;
+    snell_rel32(Ph, Qh, n, k.n_leg[i], k.n_leg[i + 1], 25, S);
+    P.valid = P.valid && S.sides && fabsf(S.res) <= kTol32;
+    for (int j = 0; j < 3; ++j) y[j] = S.y[j];
+    // upper leg |cur - x| = |(cur - o) - y|
+    const df s1 = df_norm3(df_add_f(Pd[0], -y[0]), df_add_f(Pd[1], -y[1]),
+                           df_add_f(Pd[2], -y[2]));
+    P.opl = df_add(P.opl, df_mul(s1, df_make(k.n_leg[i], k.n_leg_lo[i])));
+    const float c_inc = fmaxf(S.c1, (float)kCMin);
     if (i == 0) {
       P.c0 = c_inc;
-      for (int j = 0; j < 3; ++j) P.xf[j] = R.x[j];
+      for (int j = 0; j < 3; ++j) P.d0[j] = y[j] - Ph[j];
     }
     const float g = fresnel_gamma32(k.eps_leg[i], k.eps_leg[i + 1], c_inc);
     P.tau2 *= (1.0f - g * g);
     if (a.rough_cross) {
-      const float kt = k.k0 * (k.n_leg[i] * c_inc - k.n_leg[i + 1] * R.c2);
+      const float kt = k.k0 * (k.n_leg[i] * c_inc - k.n_leg[i + 1] * S.c2);
       const float sk = k.sig_c[i] * kt;
       P.tau2 *= __expf(-2.0f * sk * sk);
     }
-    const float s1f = (float)R.s1;
-    P.opl += a.n_leg[i] * R.s1;
+    const float s1f = s1.hi;
     P.loss_db += s1f * (k.att_leg[i] * 1e-3f);
     P.sum_perp += s1f / k.n_leg[i];
     P.sum_par += s1f / (k.n_leg[i] * c_inc * c_inc);
-    P.c_last = fmaxf(R.c2, (float)kCMin);
-    for (int j = 0; j < 3; ++j) cur[j] = R.x[j];
+    P.c_last = fmaxf(S.c2, (float)kCMin);
+    for (int j = 0; j < 3; ++j) {
+      o_prev[j] = o[j];
+      y_prev[j] = y[j];
+    }
   }
-  for (int j = 0; j < 3; ++j) P.cur[j] = cur[j];
-  double d[3] = {cur[0] - q[0], cur[1] - q[1], cur[2] - q[2]};
-  (void)d;
+  // final leg: q - x = (q - o) - y
+  const df fx = df_add_f(Qd[0], -y[0]), fy = df_add_f(Qd[1], -y[1]),
+           fz = df_add_f(Qd[2], -y[2]);
+  P.s_last = df_norm3(fx, fy, fz);
+  const float is = 1.0f / fmaxf(P.s_last.hi, 1e-30f);
+  P.rh[0] = -fx.hi * is;
+  P.rh[1] = -fy.hi * is;
+  P.rh[2] = -fz.hi * is;
 }
 
-// float32 joint solve on in-plane offsets from the local facet centres.
+// ---------------------------------------------------------------------
+// joint solve (multilayer.py:408-457, refraction_joint.py:249-322)
+// ---------------------------------------------------------------------
 template <int NI>
 __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
-                                 const double *p, const double *q,
-                                 PathS &P) {
-  // pass 1: mean-plane chain anchors the lookups (float32 + exact fallback)
+                                 const TraceS &T, const double *p64,
+                                 const float *q, PathS &P) {
+  const float *nm = k.n_leg;
+  // pass 1: mean-plane chain anchors the lookups
   int rows[NI], cols[NI];
   {
-    double cur[3] = {p[0], p[1], p[2]};
+    float Pm[3] = {T.pm0[0], T.pm0[1], T.pm0[2]};
     bool safe = true;
     for (int i = 0; i < NI; ++i) {
-      const ss_interface &I = a.ifc[i];
-      const float Pr[3] = {(float)(cur[0] - I.mean_point[0]),
-                           (float)(cur[1] - I.mean_point[1]),
-                           (float)(cur[2] - I.mean_point[2])};
-      const float Qr[3] = {(float)(q[0] - I.mean_point[0]),
-                           (float)(q[1] - I.mean_point[1]),
-                           (float)(q[2] - I.mean_point[2])};
-      const float nrm[3] = {(float)I.mean_normal[0], (float)I.mean_normal[1],
-                            (float)I.mean_normal[2]};
-      float y[3];
-      snell32_rel(Pr, Qr, nrm, k.n_leg[i], k.n_leg[i + 1], 10, y);
-      for (int j = 0; j < 3; ++j) cur[j] = I.mean_point[j] + (double)y[j];
-      const double rc0 = cur[0] * I.coef[0] + cur[1] * I.coef[2] + I.coef[4];
-      const double rc1 = cur[0] * I.coef[1] + cur[1] * I.coef[3] + I.coef[5];
-      const double f0 = rc0 - floor(rc0), f1 = rc1 - floor(rc1);
-      safe = safe && fabs(f0 - 0.5) > kLookupGuard &&
-             fabs(f1 - 0.5) > kLookupGuard;
-      rows[i] = (int)fmin(fmax(rint(rc0), 0.0), (double)(I.ny - 1));
-      cols[i] = (int)fmin(fmax(rint(rc1), 0.0), (double)(I.nx - 1));
+      const MeanPlane32 &M = k.mean[i];
+      if (i > 0)
+        for (int j = 0; j < 3; ++j) Pm[j] += M.dmp[j];
+      const float Qm[3] = {q[0] - M.mp[0], q[1] - M.mp[1], q[2] - M.mp[2]};
+      Solve32 S;
+      snell_rel32(Pm, Qm, M.mn, nm[i], nm[i + 1], 10, S);
+      safe = cell_of(M, a.ifc[i], S.y, rows[i], cols[i]) && safe;
+      for (int j = 0; j < 3; ++j) Pm[j] = S.y[j];
     }
-    if (!safe) {  // exact reference chain for this pair
-      double c64[3] = {p[0], p[1], p[2]};
-      for (int i = 0; i < NI; ++i) {
-        const ss_interface &I = a.ifc[i];
-        Snell64 R;
-        snell64(c64, q, I.mean_point, I.mean_normal, a.n_leg[i],
-                a.n_leg[i + 1], 10, false, R);
-        for (int j = 0; j < 3; ++j) c64[j] = R.x[j];
-        const double rc0 = __dadd_rn(__dadd_rn(__dmul_rn(R.x[0], I.coef[0]),
-                                               __dmul_rn(R.x[1], I.coef[2])),
-                                     I.coef[4]);
-        const double rc1 = __dadd_rn(__dadd_rn(__dmul_rn(R.x[0], I.coef[1]),
-                                               __dmul_rn(R.x[1], I.coef[3])),
-                                     I.coef[5]);
-        rows[i] = (int)fmin(fmax(rint(rc0), 0.0), (double)(I.ny - 1));
-        cols[i] = (int)fmin(fmax(rint(rc1), 0.0), (double)(I.nx - 1));
-      }
+    if (!safe) {  // the reference's float64 chain for this pair
+      double c64[3] = {p64[0], p64[1], p64[2]};
+      const double q64[3] = {q[0], q[1], q[2]};
+      for (int i = 0; i < NI; ++i)
+        cell64(a.ifc[i], c64, q64, a.n_leg[i], a.n_leg[i + 1], false, c64,
+               rows[i], cols[i]);
     }
   }
-  // local planes: float64 centres, float32 unit normals
-  double O[NI][3], N64[NI][3];
-  float Nn[NI][3];
-  for (int i = 0; i < NI; ++i) {
-    double nr[3];
-    cell_plane(a.ifc[i], rows[i], cols[i], O[i], nr);
-    const double nn = sqrt(dot3v(nr, nr));
-    for (int j = 0; j < 3; ++j) {
-      N64[i][j] = nr[j] / nn;
-      Nn[i][j] = (float)N64[i][j];
-    }
-  }
-  // segment bases: D_0 = o_0 - p, D_k = o_k - o_{k-1}, D_NI = q - o_{NI-1}
-  double D64[NI + 1][3];
+  // local planes and exact segment bases D_0 = o_0 - p, D_k = o_k - o_k-1,
+  // D_NI = q - o_NI-1
+  float O[NI][3], Nn[NI][3];
+  for (int i = 0; i < NI; ++i) cell_plane32(a.ifc[i], rows[i], cols[i], O[i],
+                                            Nn[i]);
+  df D[NI + 1][3];
+  p_minus(T, O[0], D[0]);
   for (int j = 0; j < 3; ++j) {
-    D64[0][j] = O[0][j] - p[j];
-    for (int i = 1; i < NI; ++i) D64[i][j] = O[i][j] - O[i - 1][j];
-    D64[NI][j] = q[j] - O[NI - 1][j];
+    D[0][j].hi = -D[0][j].hi;
+    D[0][j].lo = -D[0][j].lo;
+    for (int i = 1; i < NI; ++i) D[i][j] = df_diff(O[i][j], O[i - 1][j]);
+    D[NI][j] = df_diff(q[j], O[NI - 1][j]);
   }
-  double pq[3] = {p[0] - q[0], p[1] - q[1], p[2] - q[2]};
-  const float scale = (float)fmax(sqrt(dot3v(pq, pq)), kTiny);
+  float tot[3] = {0, 0, 0};
+  for (int i = 0; i <= NI; ++i)
+    for (int j = 0; j < 3; ++j) tot[j] += D[i][j].hi;
+  const float scale = fmaxf(sqrtf(dot3a(tot, tot)), kTiny32);
   const float inv = 1.0f / scale;
   float Ds[NI + 1][3];
   for (int i = 0; i <= NI; ++i)
-    for (int j = 0; j < 3; ++j) Ds[i][j] = (float)D64[i][j] * inv;
-  const float *nm = k.n_leg;
-  // chain initialiser (25 iterations), offsets y_i from o_i (scaled units)
+    for (int j = 0; j < 3; ++j) Ds[i][j] = D[i][j].hi * inv;
+  // chain initialiser (25 iterations), offsets y_i from o_i (scaled)
   float Y[NI][3];
   {
     float Qrel[NI][3];  // q - o_i = sum_{j > i} D_j
@@ -378,7 +381,9 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
       float Pr[3];
       for (int j = 0; j < 3; ++j)
         Pr[j] = i == 0 ? -Ds[0][j] : Y[i - 1][j] - Ds[i][j];
-      snell32_rel(Pr, Qrel[i], Nn[i], nm[i], nm[i + 1], 25, Y[i]);
+      Solve32 S;
+      snell_rel32(Pr, Qrel[i], Nn[i], nm[i], nm[i + 1], 25, S);
+      for (int j = 0; j < 3; ++j) Y[i][j] = S.y[j];
     }
   }
   // in-plane bases and offsets
@@ -428,33 +433,6 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
                    B[i][1][c] * (g[i][1] - g[i + 1][1]) +
                    B[i][2][c] * (g[i][2] - g[i + 1][2]);
   };
-  float dinv[NI][2][2], Cm[NI > 1 ? NI - 1 : 1][2][2];
-  // block-Thomas solve with the current factorisation (dinv, Cm)
-  auto thomas = [&](const float (&rhs_in)[NI][2], float (&delta)[NI][2]) {
-    float yv[NI][2];
-    for (int i = 0; i < NI; ++i) {
-      float rhs[2] = {rhs_in[i][0], rhs_in[i][1]};
-      if (i > 0) {
-        float cpt[2][2];
-        for (int r = 0; r < 2; ++r)
-          for (int c = 0; c < 2; ++c)
-            cpt[r][c] = Cm[i - 1][0][r] * dinv[i - 1][0][c] +
-                        Cm[i - 1][1][r] * dinv[i - 1][1][c];
-        for (int r = 0; r < 2; ++r)
-          rhs[r] -= cpt[r][0] * yv[i - 1][0] + cpt[r][1] * yv[i - 1][1];
-      }
-      yv[i][0] = rhs[0];
-      yv[i][1] = rhs[1];
-    }
-    for (int i = NI - 1; i >= 0; --i) {
-      float rr[2] = {yv[i][0], yv[i][1]};
-      if (i < NI - 1)
-        for (int r = 0; r < 2; ++r)
-          rr[r] -= Cm[i][r][0] * delta[i + 1][0] + Cm[i][r][1] * delta[i + 1][1];
-      for (int r = 0; r < 2; ++r)
-        delta[i][r] = dinv[i][r][0] * rr[0] + dinv[i][r][1] * rr[1];
-    }
-  };
   for (int it = 0; it < a.n_newton; ++it) {
     geom(ab, s, dh, f);
     float W[NI + 1][3][3];
@@ -464,7 +442,7 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
         for (int c = 0; c < 3; ++c)
           W[kk][r][c] = sc * ((r == c ? 1.0f : 0.0f) - dh[kk][r] * dh[kk][c]);
     }
-    float A[NI][2][2];
+    float A[NI][2][2], Cm[NI > 1 ? NI - 1 : 1][2][2];
     for (int i = 0; i < NI; ++i) {
       float BW[2][3];
       for (int r = 0; r < 2; ++r)
@@ -489,18 +467,22 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
                           BW[r][1] * B[i + 1][1][c] +
                           BW[r][2] * B[i + 1][2][c]);
     }
-    // factor: dinv_i = (A_i - C_{i-1}^T dinv_{i-1} C_{i-1})^-1
+    // block Thomas (refraction_joint.py:218-246)
+    float dinv[NI][2][2], yv[NI][2], delta[NI][2];
     for (int i = 0; i < NI; ++i) {
       float M[2][2] = {{A[i][0][0], A[i][0][1]}, {A[i][1][0], A[i][1][1]}};
+      float rhs[2] = {-f[i][0], -f[i][1]};
       if (i > 0) {
         float cpt[2][2];
         for (int r = 0; r < 2; ++r)
           for (int c = 0; c < 2; ++c)
             cpt[r][c] = Cm[i - 1][0][r] * dinv[i - 1][0][c] +
                         Cm[i - 1][1][r] * dinv[i - 1][1][c];
-        for (int r = 0; r < 2; ++r)
+        for (int r = 0; r < 2; ++r) {
           for (int c = 0; c < 2; ++c)
             M[r][c] -= cpt[r][0] * Cm[i - 1][0][c] + cpt[r][1] * Cm[i - 1][1][c];
+          rhs[r] -= cpt[r][0] * yv[i - 1][0] + cpt[r][1] * yv[i - 1][1];
+        }
       }
       float det = M[0][0] * M[1][1] - M[0][1] * M[1][0];
       if (fabsf(det) < kTiny32) det = kTiny32;
@@ -509,13 +491,26 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
       dinv[i][0][1] = -M[0][1] * idt;
       dinv[i][1][0] = -M[1][0] * idt;
       dinv[i][1][1] = M[0][0] * idt;
+      yv[i][0] = rhs[0];
+      yv[i][1] = rhs[1];
     }
-    float nf[NI][2], delta[NI][2];
-    for (int i = 0; i < NI; ++i) {
-      nf[i][0] = -f[i][0];
-      nf[i][1] = -f[i][1];
+    for (int i = NI - 1; i >= 0; --i) {
+      float rr[2] = {yv[i][0], yv[i][1]};
+      if (i < NI - 1)
+        for (int r = 0; r < 2; ++r)
+          rr[r] -= Cm[i][r][0] * delta[i + 1][0] + Cm[i][r][1] * delta[i + 1][1];
+      for (int r = 0; r < 2; ++r)
+        delta[i][r] = dinv[i][r][0] * rr[0] + dinv[i][r][1] * rr[1];
     }
-    thomas(nf, delta);
+    // converged to float32 resolution: take the step and stop
+    float dmax = 0.0f;
+    for (int i = 0; i < NI; ++i)
+      dmax = fmaxf(dmax, fmaxf(fabsf(delta[i][0]), fabsf(delta[i][1])));
+    if (dmax < 1e-7f) {
+      for (int i = 0; i < NI; ++i)
+        for (int r = 0; r < 2; ++r) ab[i][r] += delta[i][r];
+      break;
+    }
     float m0 = 0.0f;
     for (int i = 0; i < NI; ++i) m0 += f[i][0] * f[i][0] + f[i][1] * f[i][1];
     float lam_sel = 0.0f, lam = 1.0f;
@@ -535,70 +530,27 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
       for (int r = 0; r < 2; ++r) ab[i][r] += lam_sel * delta[i][r];
   }
   geom(ab, s, dh, f);
-  // float64 polish: tangent bases from the float64 normals, the Snell
-  // residual in float64, one Newton step through the float32 factorisation
-  // (the crossing positions enter the arrival direction at first order)
-  double B64[NI][3][2], ab64[NI][2];
-  for (int i = 0; i < NI; ++i) {
-    const double *n = N64[i];
-    const bool use_z = fabs(n[2]) < 0.9;
-    const double a0 = use_z ? 0.0 : 1.0, a2 = use_z ? 1.0 : 0.0;
-    double u[3] = {-a2 * n[1], a2 * n[0] - a0 * n[2], a0 * n[1]};
-    const double un = 1.0 / sqrt(dot3v(u, u));
-    for (int j = 0; j < 3; ++j) u[j] *= un;
-    const double v[3] = {n[1] * u[2] - n[2] * u[1], n[2] * u[0] - n[0] * u[2],
-                         n[0] * u[1] - n[1] * u[0]};
+  // crossings in metres from their facet centres; exact segment lengths
+  float Ym[NI][3];
+  for (int i = 0; i < NI; ++i)
+    for (int j = 0; j < 3; ++j)
+      Ym[i][j] = scale * (B[i][j][0] * ab[i][0] + B[i][j][1] * ab[i][1]);
+  df S[NI + 1];
+  df seg_last[3];
+  for (int kk = 0; kk <= NI; ++kk) {
+    df v[3];
     for (int j = 0; j < 3; ++j) {
-      B64[i][j][0] = u[j];
-      B64[i][j][1] = v[j];
+      v[j] = D[kk][j];
+      if (kk < NI) v[j] = df_add_f(v[j], Ym[kk][j]);
+      if (kk > 0) v[j] = df_add_f(v[j], -Ym[kk - 1][j]);
     }
-    // re-express the float32 offset in the float64 basis
-    const double y[3] = {
-        (double)(B[i][0][0] * ab[i][0] + B[i][0][1] * ab[i][1]),
-        (double)(B[i][1][0] * ab[i][0] + B[i][1][1] * ab[i][1]),
-        (double)(B[i][2][0] * ab[i][0] + B[i][2][1] * ab[i][1])};
-    for (int c = 0; c < 2; ++c)
-      ab64[i][c] = B64[i][0][c] * y[0] + B64[i][1][c] * y[1] +
-                   B64[i][2][c] * y[2];
+    S[kk] = df_norm3(v[0], v[1], v[2]);
+    if (kk == 0)
+      for (int j = 0; j < 3; ++j) P.d0[j] = v[j].hi;
+    if (kk == NI)
+      for (int j = 0; j < 3; ++j) seg_last[j] = v[j];
   }
-  const double scale64 = (double)scale;
-  double X[NI][3], S64[NI + 1];
-  auto geom64 = [&](bool want_f, float (&fo)[NI][2]) {
-    for (int i = 0; i < NI; ++i)
-      for (int j = 0; j < 3; ++j)
-        X[i][j] = O[i][j] + scale64 * (B64[i][j][0] * ab64[i][0] +
-                                       B64[i][j][1] * ab64[i][1]);
-    double g[NI + 1][3];
-    for (int kk = 0; kk <= NI; ++kk) {
-      const double *pa = kk == 0 ? p : X[kk - 1];
-      const double *pb = kk == NI ? q : X[kk];
-      double d[3] = {pb[0] - pa[0], pb[1] - pa[1], pb[2] - pa[2]};
-      S64[kk] = sqrt(dot3v(d, d));
-      const double gs = a.n_leg[kk] / fmax(S64[kk], kTiny);
-      for (int j = 0; j < 3; ++j) g[kk][j] = gs * d[j];
-    }
-    if (want_f)
-      for (int i = 0; i < NI; ++i)
-        for (int c = 0; c < 2; ++c)
-          fo[i][c] = -(float)(B64[i][0][c] * (g[i][0] - g[i + 1][0]) +
-                              B64[i][1][c] * (g[i][1] - g[i + 1][1]) +
-                              B64[i][2][c] * (g[i][2] - g[i + 1][2]));
-  };
-  float nf64[NI][2];
-  geom64(a.n_newton > 0, nf64);
-  if (a.n_newton > 0) {
-    float d64[NI][2];
-    thomas(nf64, d64);
-    bool fin = true;
-    for (int i = 0; i < NI; ++i) fin = fin && isfinite(d64[i][0]) &&
-                                       isfinite(d64[i][1]);
-    if (fin) {
-      for (int i = 0; i < NI; ++i)
-        for (int c = 0; c < 2; ++c) ab64[i][c] += (double)d64[i][c];
-      geom64(false, nf64);
-    }
-  }
-  // validity (float32): residual, straddling, evanescence
+  // validity: residual, straddling, evanescence (refraction_joint:143-176)
   float residual = 0.0f;
   bool sides = true, evan = false;
   float cinc[NI], cout_[NI];
@@ -618,17 +570,16 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
     const float rt[3] = {dG[0] - nd * n[0], dG[1] - nd * n[1], dG[2] - nd * n[2]};
     const float res = sqrtf(dot3a(rt, rt));
     if (res > residual || isnan(res)) residual = res;
-    // P_i - x_i = -seg_i, P_{i+2} - x_i = seg_{i+1} (unit directions suffice)
     sides = sides && (-dot3a(n, dh[i]) * dot3a(n, dh[i + 1]) < 0.0f);
     evan = evan || (nm[i] * st1 > nm[i + 1] * (1.0f + 64.0f * kEps32));
   }
   P.valid = (residual <= kTol32) && isfinite(residual) && sides && !evan;
-  // radiometry sums (multilayer.py:436-457)
+  // radiometry sums and optical path (multilayer.py:436-457)
   float c_inc[NI];
   for (int i = 0; i < NI; ++i) c_inc[i] = fmaxf(cinc[i], (float)kCMin);
   const float c_surf = c_inc[a.k_pad];
   float tau2 = 1.0f, loss = 0.0f, sperp = 0.0f, spar = 0.0f;
-  double opl = 0.0;
+  df opl = df_make(0.0f, 0.0f);
   for (int i = 0; i < NI; ++i) {
     const float g = fresnel_gamma32(k.eps_leg[i], k.eps_leg[i + 1], c_inc[i]);
     tau2 *= (1.0f - g * g);
@@ -638,8 +589,8 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
       tau2 *= __expf(-2.0f * sk * sk);
     }
     const float cp = i < a.k_pad ? c_surf : c_inc[i];
-    const float si = (float)S64[i];
-    opl += a.n_leg[i] * S64[i];
+    const float si = S[i].hi;
+    opl = df_add(opl, df_mul(S[i], df_make(k.n_leg[i], k.n_leg_lo[i])));
     loss += si * (k.att_leg[i] * 1e-3f);
     sperp += si / nm[i];
     spar += si / (nm[i] * cp * cp);
@@ -651,10 +602,9 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
   P.sum_par = spar;
   P.c0 = c_surf;
   P.c_last = fmaxf(cout_[NI - 1], (float)kCMin);
-  for (int j = 0; j < 3; ++j) {
-    P.cur[j] = X[NI - 1][j];
-    P.xf[j] = X[0][j];
-  }
+  P.s_last = S[NI];
+  const float is = 1.0f / fmaxf(S[NI].hi, 1e-30f);
+  for (int j = 0; j < 3; ++j) P.rh[j] = -seg_last[j].hi * is;
 }
 
 template <int NI, int ROUGH>
@@ -663,7 +613,8 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *hist = reinterpret_cast<float2 *>(smem_raw);
   float *lg = reinterpret_cast<float *>(hist + (size_t)a.tb * a.n_seg);
-  __shared__ double s_p[SS_MAX_TB][3];
+  __shared__ double s_p64[SS_MAX_TB][3];
+  __shared__ TraceS s_tr[SS_MAX_TB];
   __shared__ float s_u[SS_MAX_TB][3], s_pv[SS_MAX_TB][6];
   __shared__ int s_lo[SS_MAX_TB], s_hi[SS_MAX_TB];
   __shared__ float s_drop[SS_MAX_TB];
@@ -682,7 +633,12 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   if (tid < nt) {
     const int t = t_base + tid;
     for (int j = 0; j < 3; ++j) {
-      s_p[tid][j] = a.pos[3 * t + j];
+      const double pj = a.pos[3 * t + j];
+      s_p64[tid][j] = pj;
+      const df v = df_from_double(pj);
+      s_tr[tid].ph[j] = v.hi;
+      s_tr[tid].pl[j] = v.lo;
+      s_tr[tid].pm0[j] = (float)(pj - a.ifc[0].mean_point[j]);
       s_u[tid][j] = a.uct ? (float)a.uct[3 * t + j] : 0.0f;
     }
     for (int j = 0; j < 6; ++j)
@@ -719,28 +675,23 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
 
   const int nj = a.leg_last;
   const float n0 = k.n_leg[0], njn = k.n_leg[nj];
+  const df njd = df_make(k.n_leg[nj], k.n_leg_lo[nj]);
   const float nsf = (float)a.n_samples;
   for (int i = s_rng[0] + tid; i < s_rng[1]; i += blockDim.x) {
-    const double q[3] = {(double)a.F.cx[i], (double)a.F.cy[i],
-                         (double)a.F.cz[i]};
+    const float q[3] = {a.F.cx[i], a.F.cy[i], a.F.cz[i]};
     const float fn[3] = {a.F.nx[i], a.F.ny[i], a.F.nz[i]};
     const float fa = a.F.area[i];
     for (int tt = 0; tt < nt; ++tt) {
       if (i < s_lo[tt] || i >= s_hi[tt]) continue;
       PathS P;
       if (NI == 0)
-        path_sequential_split(a, k, s_p[tt], q, P);
+        path_sequential_split(a, k, s_tr[tt], s_p64[tt], q, P);
       else
-        path_joint_split<NI == 0 ? 1 : NI>(a, k, s_p[tt], q, P);
-      // final leg: crossing -> facet, float64 length for the optical path
-      const double d64[3] = {P.cur[0] - q[0], P.cur[1] - q[1],
-                             P.cur[2] - q[2]};
-      const double s_j64 = sqrt(dot3v(d64, d64));
-      const double opl = P.opl + a.n_leg[nj] * s_j64;
-      const float s_j = (float)s_j64;
-      const float inv = 1.0f / fmaxf(s_j, 1e-30f);
-      const float rh[3] = {(float)d64[0] * inv, (float)d64[1] * inv,
-                           (float)d64[2] * inv};
+        path_joint_split<NI == 0 ? 1 : NI>(a, k, s_tr[tt], s_p64[tt], q, P);
+      // final leg (medium j)
+      const df opl = df_add(P.opl, df_mul(P.s_last, njd));
+      const float s_j = P.s_last.hi;
+      const float *rh = P.rh;
       const float loss = P.loss_db + s_j * (k.att_leg[nj] * 1e-3f);
       const float sperp = P.sum_perp + s_j / njn;
       const float spar = P.sum_par + s_j / (njn * P.c_last * P.c_last);
@@ -751,26 +702,18 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
       const float cos_t = dot3a(rh, fn);
       float spread = P.tau2 * flux / (l_par * l_perp);
       if (a.pat_kind != SS_PAT_ISOTROPIC) {
-        const float d0[3] = {(float)(P.xf[0] - s_p[tt][0]),
-                             (float)(P.xf[1] - s_p[tt][1]),
-                             (float)(P.xf[2] - s_p[tt][2])};
-        const float dm = rsqrtf(fmaxf(dot3a(d0, d0), 1e-30f));
+        const float dm = rsqrtf(fmaxf(dot3a(P.d0, P.d0), 1e-30f));
         const float g = gain32(a.pat_kind, a.pat_n, pa_len, s_pat, s_pv[tt],
-                               d0[0] * dm, d0[1] * dm, d0[2] * dm);
+                               P.d0[0] * dm, P.d0[1] * dm, P.d0[2] * dm);
         spread *= g * g;
       }
       float re, im, pwr;
       if (a.coherent) {
-        const float gam = a.F.gamma_f64 ? (float)a.F.gamma_f64[i] : (float)a.gamma;
+        const float gam = a.F.gamma_f64 ? (float)a.F.gamma_f64[i]
+                                        : (float)a.gamma;
         const float f1[3] = {a.F.e1x[i], a.F.e1y[i], a.F.e1z[i]};
         const float f2[3] = {a.F.e2x[i], a.F.e2y[i], a.F.e2z[i]};
-        // r_hat . e in float64: the sinc arguments k_j (r_hat . e) need the
-        // arrival direction to ~1e-8 rad
-        const double is64 = 1.0 / fmax(s_j64, 1e-30);
-        const float d1 = (float)((d64[0] * (double)f1[0] + d64[1] * (double)f1[1] +
-                                  d64[2] * (double)f1[2]) * is64);
-        const float d2 = (float)((d64[0] * (double)f2[0] + d64[1] * (double)f2[1] +
-                                  d64[2] * (double)f2[2]) * is64);
+        const float d1 = dot3a(rh, f1), d2 = dot3a(rh, f2);
         const float base = k.amp_pref_j * gam * cos_t * spread * att_f;
         float amp = base * fa * sinc32(k.kj * d1) * sinc32(k.kj * d2);
         if (a.taper) {
@@ -805,10 +748,13 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
           cr += ad * a.F.diffuse_phasor[2 * i];
           ci += ad * a.F.diffuse_phasor[2 * i + 1];
         }
-        // carrier phase 2 k0 opl reduced modulo 2 pi in float64
-        const double ph = 2.0 * a.k0 * opl;
-        const double nred = rint(ph * 0.15915494309189535);
-        const float red = (float)fma(-nred, 6.283185307179586, ph);
+        // carrier phase 2 k0 opl mod 2 pi (double-float, Cody-Waite)
+        float ph, pe;
+        two_prod(k.K2h, opl.hi, ph, pe);
+        const float pl = pe + __fmaf_rn(k.K2h, opl.lo, k.K2l * opl.hi);
+        const float n2 = rintf(ph * 0.159154943091895336f);
+        float red = __fmaf_rn(-n2, 6.28318548202514648f, ph);  // exact
+        red = __fmaf_rn(-n2, -1.74845553146951e-07f, red) + pl;
         float sn, cs;
         __sincosf(red, &sn, &cs);
         re = cr * sn - ci * cs;
@@ -820,25 +766,30 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
         im = 0.0f;
         pwr = re;
       }
-      // fast-time bin from the float64 optical path; exact path near edges
-      const double u = (2.0 * opl / a.c - a.t0) / a.dt;
-      double fb = floor(u);
-      const float frac = (float)(u - fb);
-      bool valid = P.valid;
-      if ((frac < kBinGuard || frac > 1.0f - kBinGuard) && u > -4.0 &&
-          u < (double)a.n_samples + 4.0) {
+      // fast-time bin u = opl A - B (double-float), float64 path near edges
+      float up, ue, us, ue2;
+      two_prod(opl.hi, k.Ah, up, ue);
+      two_sum(up, -k.Bh, us, ue2);
+      const float ul = (ue2 + ue) + __fmaf_rn(opl.hi, k.Al, opl.lo * k.Ah) -
+                       k.Bl;
+      float fb = floorf(us);
+      float frac = (us - fb) + ul;
+      if (frac < 0.0f) { fb -= 1.0f; frac += 1.0f; }
+      else if (frac >= 1.0f) { fb += 1.0f; frac -= 1.0f; }
+      if ((frac < kBinGuard || frac > 1.0f - kBinGuard) && us > -4.0f &&
+          us < nsf + 4.0f) {
         bool v64;
-        const double o64 = full_opl64<NI>(a, s_p[tt], q, v64);
+        const double q64[3] = {q[0], q[1], q[2]};
+        const double o64 = full_opl64<NI>(a, s_p64[tt], q64, v64);
         const double twtt = __ddiv_rn(__dmul_rn(2.0, o64), a.c);
-        fb = floor(__ddiv_rn(__dsub_rn(twtt, a.t0), a.dt));
+        fb = (float)floor(__ddiv_rn(__dsub_rn(twtt, a.t0), a.dt));
       }
-      const bool ok = valid && fb >= 0.0 && fb < (double)nsf;
+      const bool ok = P.valid && fb >= 0.0f && fb < nsf;
       if (ok) {
         int b = (int)fb;
         if (a.split) {
-          const float v[3] = {(float)(q[0] - s_p[tt][0]),
-                              (float)(q[1] - s_p[tt][1]),
-                              (float)(q[2] - s_p[tt][2])};
+          const float v[3] = {q[0] - s_tr[tt].ph[0], q[1] - s_tr[tt].ph[1],
+                              q[2] - s_tr[tt].ph[2]};
           if (dot3a(v, s_u[tt]) > 0.0f) b += a.n_samples;
         }
         float2 *h = hist + (size_t)tt * a.n_seg + b;
@@ -910,12 +861,41 @@ int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
   k.corr = (float)a.corr;
   k.fadL = (float)a.fad.L;
   k.n_exp = (float)a.n_exp;
+  const df k2 = df_from_double(2.0 * a.k0);
+  k.K2h = k2.hi;
+  k.K2l = k2.lo;
+  const df A = df_from_double(2.0 / (a.c * a.dt));
+  const df B = df_from_double(a.t0 / a.dt);
+  k.Ah = A.hi;
+  k.Al = A.lo;
+  k.Bh = B.hi;
+  k.Bl = B.lo;
   for (int i = 0; i <= a.leg_last; ++i) {
-    k.n_leg[i] = (float)a.n_leg[i];
+    const df n = df_from_double(a.n_leg[i]);
+    k.n_leg[i] = n.hi;
+    k.n_leg_lo[i] = n.lo;
     k.eps_leg[i] = (float)a.eps_leg[i];
     k.att_leg[i] = (float)a.att_leg[i];
   }
-  for (int i = 0; i < a.ni; ++i) k.sig_c[i] = (float)a.sig_c[i];
+  for (int i = 0; i < a.ni; ++i) {
+    const ss_interface &I = a.ifc[i];
+    MeanPlane32 &M = k.mean[i];
+    k.sig_c[i] = (float)a.sig_c[i];
+    for (int j = 0; j < 3; ++j) {
+      M.mp[j] = (float)I.mean_point[j];
+      M.mn[j] = (float)I.mean_normal[j];
+      M.dmp[j] = i == 0 ? 0.0f
+                        : (float)(a.ifc[i - 1].mean_point[j] - I.mean_point[j]);
+    }
+    M.coef[0] = (float)I.coef[0];
+    M.coef[1] = (float)I.coef[1];
+    M.coef[2] = (float)I.coef[2];
+    M.coef[3] = (float)I.coef[3];
+    M.rb[0] = (float)(I.mean_point[0] * I.coef[0] +
+                      I.mean_point[1] * I.coef[2] + I.coef[4]);
+    M.rb[1] = (float)(I.mean_point[0] * I.coef[1] +
+                      I.mean_point[1] * I.coef[3] + I.coef[5]);
+  }
   const size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2) +
                       (a.rough_kind ? (a.n_terms + 1) * sizeof(float) : 0);
   if (!a.joint) return launch_split_r<0>(a, k, p, smem, st);
