@@ -24,7 +24,7 @@ __device__ __forceinline__ double dot3v(const double *a, const double *b) {
 // form of multilayer.py:196-266).
 static __device__ __noinline__ void snell64(const double *p, const double *q, const double *o,
                         const double *nrm, double n1, double n2, int n_iter,
-                        bool comp, Snell64 &R) {
+                        bool comp, Snell64 &R, bool early = false) {
   double po[3] = {p[0] - o[0], p[1] - o[1], p[2] - o[2]};
   double qo[3] = {q[0] - o[0], q[1] - o[1], q[2] - o[2]};
   const double h1 = dot3v(po, nrm), h2 = dot3v(qo, nrm);
@@ -63,7 +63,12 @@ static __device__ __noinline__ void snell64(const double *p, const double *q, co
     const double Fp = ar / (c1 * sc1) + (bd * ratio) / (c2 * sc2);
     const double sn = sig - F / fmax(Fp, kTiny);
     const bool ok = (sn >= lo) && (sn <= hi) && isfinite(sn);
-    sig = ok ? sn : 0.5 * (lo + hi);
+    const double nxt = ok ? sn : 0.5 * (lo + hi);
+    // early: stop at the fixed point (the remaining fixed-budget iterations
+    // would leave sigma unchanged to within an ulp)
+    const bool done = early && fabs(nxt - sig) <= 4.0 * kEps64 * fmax(sig, 1e-12);
+    sig = nxt;
+    if (done) break;
   }
   const double c1 = fmax((1.0 - sig) * (1.0 + sig), kTiny);
   const double tr = comp ? ar * sig * (1.0 / sqrt(c1)) : ar * sig / sqrt(c1);

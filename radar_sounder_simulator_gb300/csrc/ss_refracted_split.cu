@@ -15,7 +15,8 @@
 //     crossing to micrometres, which keeps the facet's arrival direction --
 //     and the sinc arguments k_j (r_hat . e) -- accurate to ~1e-8 rad;
 //   * facet lookups: the float32 mean-plane crossing gives the affine cell
-//     coordinate; if it lies within 1e-3 cells of a rounding boundary the
+//     coordinate (formed as a double-float; the crossing itself carries
+//     ~2e-5 cells of float32 error); within 3e-4 cells of a rounding boundary the
 //     float64 mean-plane chain of the reference is re-run for that pair, so
 //     the lookups are the reference's integer decisions;
 //   * leg lengths, optical path, carrier phase (2 k0 opl mod 2 pi) and the
@@ -38,7 +39,7 @@ namespace ss {
 constexpr float kTiny32 = 1e-30f;
 constexpr float kEps32 = 1.1920929e-07f;
 constexpr float kTol32 = 1e-4f;
-constexpr float kLookupGuard = 1e-3f;
+constexpr float kLookupGuard = 3e-4f;
 constexpr float kBinGuard = 1e-6f;
 
 // Per-interface constants of the float32 lookup pass.
@@ -47,7 +48,9 @@ struct MeanPlane32 {
   float mn[3];    // unit mean normal
   float dmp[3];   // mean point of the interface above minus this one
   float coef[4];  // affine fit: row = c0 x + c2 y + rb0, col = c1 x + c3 y + rb1
-  float rb[2];    // affine value at the mean point
+  float coefl[4]; // low parts of the coefficients (double-float)
+  float rb[2];    // affine value at the mean point (double-float hi)
+  float rbl[2];   // ... and lo
 };
 
 struct RefSplitConsts {
@@ -155,12 +158,29 @@ __device__ __forceinline__ void snell_rel32(const float *P, const float *Q,
 __device__ __forceinline__ bool cell_of(const MeanPlane32 &M,
                                         const ss_interface &I, const float *y,
                                         int &row, int &col) {
-  const float rc0 = M.rb[0] + (y[0] * M.coef[0] + y[1] * M.coef[2]);
-  const float rc1 = M.rb[1] + (y[0] * M.coef[1] + y[1] * M.coef[3]);
-  const float f0 = rc0 - floorf(rc0), f1 = rc1 - floorf(rc1);
-  row = (int)fminf(fmaxf(rintf(rc0), 0.0f), (float)(I.ny - 1));
-  col = (int)fminf(fmaxf(rintf(rc1), 0.0f), (float)(I.nx - 1));
-  return fabsf(f0 - 0.5f) > kLookupGuard && fabsf(f1 - 0.5f) > kLookupGuard;
+  // rc = rb + y . coef as a double-float (the float32 sum of ~500-cell
+  // terms would carry ~3e-5 cells of rounding)
+  float f[2];
+  int idx[2];
+  for (int c = 0; c < 2; ++c) {
+    float p0, e0, p1, e1, s0, es, s1, es1;
+    two_prod(y[0], M.coef[c], p0, e0);
+    two_prod(y[1], M.coef[2 + c], p1, e1);
+    two_sum(p0, p1, s0, es);
+    two_sum(M.rb[c], s0, s1, es1);
+    const float lo = (es1 + es) + (e0 + e1) + M.rbl[c] +
+                     (y[0] * M.coefl[c] + y[1] * M.coefl[2 + c]);
+    const float fl = floorf(s1);
+    float fr = (s1 - fl) + lo;  // in [-small, 1 + small)
+    float base = fl;
+    if (fr < 0.0f) { base -= 1.0f; fr += 1.0f; }
+    else if (fr >= 1.0f) { base += 1.0f; fr -= 1.0f; }
+    f[c] = fr;
+    idx[c] = (int)(base + (fr >= 0.5f ? 1.0f : 0.0f));
+  }
+  row = min(max(idx[0], 0), I.ny - 1);
+  col = min(max(idx[1], 0), I.nx - 1);
+  return fabsf(f[0] - 0.5f) > kLookupGuard && fabsf(f[1] - 0.5f) > kLookupGuard;
 }
 
 // Exact reference cell from a float64 mean-plane solve (multilayer.py
@@ -170,7 +190,7 @@ __device__ __noinline__ void cell64(const ss_interface &I, const double *cur,
                                     bool comp, double *x_out, int &row,
                                     int &col) {
   Snell64 R;
-  snell64(cur, q, I.mean_point, I.mean_normal, n1, n2, 10, comp, R);
+  snell64(cur, q, I.mean_point, I.mean_normal, n1, n2, 10, comp, R, true);
   const double rc0 = __dadd_rn(__dadd_rn(__dmul_rn(R.x[0], I.coef[0]),
                                          __dmul_rn(R.x[1], I.coef[2])),
                                I.coef[4]);
@@ -887,14 +907,18 @@ int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
       M.dmp[j] = i == 0 ? 0.0f
                         : (float)(a.ifc[i - 1].mean_point[j] - I.mean_point[j]);
     }
-    M.coef[0] = (float)I.coef[0];
-    M.coef[1] = (float)I.coef[1];
-    M.coef[2] = (float)I.coef[2];
-    M.coef[3] = (float)I.coef[3];
-    M.rb[0] = (float)(I.mean_point[0] * I.coef[0] +
-                      I.mean_point[1] * I.coef[2] + I.coef[4]);
-    M.rb[1] = (float)(I.mean_point[0] * I.coef[1] +
-                      I.mean_point[1] * I.coef[3] + I.coef[5]);
+    for (int c = 0; c < 4; ++c) {
+      const df cd = df_from_double(I.coef[c]);
+      M.coef[c] = cd.hi;
+      M.coefl[c] = cd.lo;
+    }
+    for (int c = 0; c < 2; ++c) {
+      const double rbv = (double)M.mp[0] * I.coef[c] +
+                         (double)M.mp[1] * I.coef[2 + c] + I.coef[4 + c];
+      const df r = df_from_double(rbv);
+      M.rb[c] = r.hi;
+      M.rbl[c] = r.lo;
+    }
   }
   const size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2) +
                       (a.rough_kind ? (a.n_terms + 1) * sizeof(float) : 0);
