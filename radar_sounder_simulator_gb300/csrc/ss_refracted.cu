@@ -199,7 +199,7 @@ static int refracted_plan(const ss_refracted_opts *o, int T, int N, Plan *p) {
   tb = std::min(tb, T);
   p->tb = tb;
   p->n_groups = (T + tb - 1) / tb;
-  p->threads = 128;
+  p->threads = o->precision == SS_PREC_FP64 ? 128 : kSplitThreads;
   const long window = std::min<long>((long)o->n_win * o->block_size, N);
   const int max_chunks = (int)std::max<long>(1, window / 256);
   const int target = 8 * sm_count();
@@ -209,6 +209,16 @@ static int refracted_plan(const ss_refracted_opts *o, int T, int N, Plan *p) {
   return SS_OK;
 }
 
+// Deferral bitmask of the split form: one bit per (trace, window slot).
+static long long defer_slots(const ss_refracted_opts *o, int N) {
+  return std::min<long long>((long long)o->n_win * o->block_size, N);
+}
+
+static size_t defer_mask_bytes(const ss_refracted_opts *o, int T, int N) {
+  const unsigned long long bits = (unsigned long long)T * defer_slots(o, N);
+  return (size_t)((bits + 31) / 32) * sizeof(uint32_t);
+}
+
 static size_t refracted_scratch(const ss_refracted_opts *o, int T, int N) {
   Plan p;
   if (refracted_plan(o, T, N, &p) != SS_OK) return 0;
@@ -216,7 +226,10 @@ static size_t refracted_scratch(const ss_refracted_opts *o, int T, int N) {
   const size_t elt = o->precision == SS_PREC_FP64 ? 16 : 8;
   size_t hist = (size_t)p.n_chunks * T * n_seg * elt;
   hist = (hist + 255) & ~(size_t)255;
-  return hist + (size_t)p.n_chunks * T * sizeof(double);
+  size_t drop = (size_t)p.n_chunks * T * sizeof(double);
+  if (o->precision == SS_PREC_FP64) return hist + drop;
+  drop = (drop + 255) & ~(size_t)255;
+  return hist + drop + defer_mask_bytes(o, T, N);
 }
 
 template <int NI>
@@ -361,6 +374,13 @@ extern "C" int ss_refracted_fwd(const ss_refracted_opts *opts,
   hist = (hist + 255) & ~(size_t)255;
   a.part_drop = reinterpret_cast<double *>(static_cast<char *>(scratch) +
                                            hist);
+  if (opts->precision != SS_PREC_FP64) {
+    const size_t drop =
+        ((size_t)p.n_chunks * T * sizeof(double) + 255) & ~(size_t)255;
+    a.defer_mask = reinterpret_cast<uint32_t *>(static_cast<char *>(scratch) +
+                                                hist + drop);
+    a.defer_w = defer_slots(opts, N);
+  }
   a.tb = p.tb;
   a.n_chunks = p.n_chunks;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -27,7 +27,14 @@ struct RefArgs {
   int tb, n_chunks;
   void *part;
   double *part_drop;
+  // split form: one bit per (trace, window slot) for pairs deferred to the
+  // fix-up kernel; defer_w = window slots per trace
+  uint32_t *defer_mask;
+  long long defer_w;
 };
+
+// Threads per CTA of the split fast kernel (its __launch_bounds__).
+constexpr int kSplitThreads = 512;
 
 int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st);
 

@@ -237,6 +237,7 @@ struct PathS {
   float d0[3];         // platform -> first crossing
   float loss_db, sum_par, sum_perp, tau2, c0, c_last;
   bool valid;
+  bool defer;          // needs the float64 lookup chain (EXACT = false only)
 };
 
 // p - o as a double-float vector (o a float point).
@@ -252,6 +253,7 @@ __device__ __forceinline__ void p_minus(const TraceS &T, const float *o,
 // ---------------------------------------------------------------------
 // sequential chain (multilayer.py:352-406)
 // ---------------------------------------------------------------------
+template <bool EXACT>
 __device__ void path_sequential_split(const RefArgs &a,
                                       const RefSplitConsts &k,
                                       const TraceS &T, const double *p64,
@@ -260,6 +262,7 @@ __device__ void path_sequential_split(const RefArgs &a,
   df Pd[3], Qd[3];
   float y[3] = {0, 0, 0};
   P.valid = true;
+  P.defer = false;
   P.opl = df_make(0.0f, 0.0f);
   P.loss_db = P.sum_par = P.sum_perp = 0.0f;
   P.tau2 = 1.0f;
@@ -277,6 +280,10 @@ __device__ void path_sequential_split(const RefArgs &a,
     snell_rel32(Pm, Qm, M.mn, k.n_leg[i], k.n_leg[i + 1], 10, Sm);
     int row, col;
     if (!cell_of(M, I, Sm.y, row, col)) {
+      if (!EXACT) {
+        P.defer = true;
+        return;
+      }
       double cur64[3], q64[3] = {q[0], q[1], q[2]}, x1[3];
       for (int j = 0; j < 3; ++j)
         cur64[j] = i == 0 ? p64[j] : (double)o_prev[j] + (double)y_prev[j];
@@ -337,11 +344,12 @@ __device__ void path_sequential_split(const RefArgs &a,
 // ---------------------------------------------------------------------
 // joint solve (multilayer.py:408-457, refraction_joint.py:249-322)
 // ---------------------------------------------------------------------
-template <int NI>
+template <int NI, bool EXACT>
 __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
                                  const TraceS &T, const double *p64,
                                  const float *q, PathS &P) {
   const float *nm = k.n_leg;
+  P.defer = false;
   // pass 1: mean-plane chain anchors the lookups
   int rows[NI], cols[NI];
   {
@@ -358,6 +366,10 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
       for (int j = 0; j < 3; ++j) Pm[j] = S.y[j];
     }
     if (!safe) {  // the reference's float64 chain for this pair
+      if (!EXACT) {
+        P.defer = true;
+        return;
+      }
       double c64[3] = {p64[0], p64[1], p64[2]};
       const double q64[3] = {q[0], q[1], q[2]};
       for (int i = 0; i < NI; ++i)
@@ -627,8 +639,179 @@ __device__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
   for (int j = 0; j < 3; ++j) P.rh[j] = -seg_last[j].hi * is;
 }
 
+// Antenna table lengths (pa, pb) of a pattern kind.
+__host__ __device__ __forceinline__ void pattern_lengths(int kind, int n,
+                                                         int &pa_len,
+                                                         int &pb_len) {
+  pa_len = pb_len = 0;
+  if (kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
+  if (kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
+  if (kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * n; pb_len = 4; }
+  if (kind == SS_PAT_TABULATED) { pa_len = n; pb_len = n; }
+}
+
+// Platform data of trace t in the split kernels' form.
+__device__ __forceinline__ void load_trace(const RefArgs &a, int t, TraceS &T,
+                                           double *p64, float *u, float *pv) {
+  for (int j = 0; j < 3; ++j) {
+    const double pj = a.pos[3 * t + j];
+    p64[j] = pj;
+    const df v = df_from_double(pj);
+    T.ph[j] = v.hi;
+    T.pl[j] = v.lo;
+    T.pm0[j] = (float)(pj - a.ifc[0].mean_point[j]);
+    u[j] = a.uct ? (float)a.uct[3 * t + j] : 0.0f;
+  }
+  for (int j = 0; j < 6; ++j)
+    pv[j] = (a.pv && j < a.pv_len) ? (float)a.pv[a.pv_len * t + j] : 0.0f;
+}
+
+// Result of one (trace, facet) pair.
+struct PairOut {
+  float re, im, pwr;
+  int bin;  // segment index, or -1 when the pair is dropped
+};
+
+// One (trace, facet) pair of the split form (multilayer.py:459-588 per
+// pair). With EXACT = false the pair returns false, without a result, when
+// it needs a float64 decision: a facet lookup or a fast-time bin within the
+// guard band of a rounding boundary. The fast kernel holds no float64 code
+// (which halves its registers) and leaves those pairs -- a few per thousand
+// -- to the fix-up kernel, which evaluates them with EXACT = true.
+template <int NI, int ROUGH, bool EXACT>
+__device__ __forceinline__ bool pair_eval(
+    const RefArgs &a, const RefSplitConsts &k, const TraceS &T,
+    const double *p64, const float *u, const float *pv, const float *pat,
+    int pa_len, const float *lg, const float *fad, int i, const float *q,
+    PairOut &o) {
+  PathS P;
+  if (NI == 0)
+    path_sequential_split<EXACT>(a, k, T, p64, q, P);
+  else
+    path_joint_split<NI == 0 ? 1 : NI, EXACT>(a, k, T, p64, q, P);
+  if (!EXACT && P.defer) return false;
+  const int nj = a.leg_last;
+  const float n0 = k.n_leg[0], njn = k.n_leg[nj];
+  const float nsf = (float)a.n_samples;
+  const float fn[3] = {a.F.nx[i], a.F.ny[i], a.F.nz[i]};
+  const float fa = a.F.area[i];
+  // final leg (medium j)
+  const df opl = df_add(P.opl, df_mul(P.s_last, df_make(k.n_leg[nj],
+                                                        k.n_leg_lo[nj])));
+  const float s_j = P.s_last.hi;
+  const float *rh = P.rh;
+  const float loss = P.loss_db + s_j * (k.att_leg[nj] * 1e-3f);
+  const float sperp = P.sum_perp + s_j / njn;
+  const float spar = P.sum_par + s_j / (njn * P.c_last * P.c_last);
+  const float l_perp = n0 * sperp;
+  const float l_par = n0 * P.c0 * P.c0 * spar;
+  const float flux = (n0 * P.c0) / (njn * P.c_last);
+  const float att_f = exp2f(-loss * 0.33219280949f);  // 10^(-loss/10)
+  const float cos_t = dot3a(rh, fn);
+  float spread = P.tau2 * flux / (l_par * l_perp);
+  if (a.pat_kind != SS_PAT_ISOTROPIC) {
+    const float dm = rsqrtf(fmaxf(dot3a(P.d0, P.d0), 1e-30f));
+    const float g = gain32(a.pat_kind, a.pat_n, pa_len, pat, pv,
+                           P.d0[0] * dm, P.d0[1] * dm, P.d0[2] * dm);
+    spread *= g * g;
+  }
+  float re, im, pwr;
+  if (a.coherent) {
+    const float gam = a.F.gamma_f64 ? (float)a.F.gamma_f64[i]
+                                    : (float)a.gamma;
+    const float f1[3] = {a.F.e1x[i], a.F.e1y[i], a.F.e1z[i]};
+    const float f2[3] = {a.F.e2x[i], a.F.e2y[i], a.F.e2z[i]};
+    const float d1 = dot3a(rh, f1), d2 = dot3a(rh, f2);
+    const float base = k.amp_pref_j * gam * cos_t * spread * att_f;
+    float amp = base * fa * sinc32(k.kj * d1) * sinc32(k.kj * d2);
+    if (a.taper) {
+      const float ct = fminf(fmaxf(cos_t, (float)kCMin), 1.0f);
+      const float ct2 = ct * ct;
+      amp *= __expf(-__fdividef(1.0f - ct2, ct2) * k.taper_inv);
+    }
+    float cr = amp, ci = 0.0f;
+    if (ROUGH != SS_ROUGH_NONE) {
+      const float sg = a.F.sigma ? a.F.sigma[i] : k.sigma;
+      const float lc = a.F.corr ? a.F.corr[i] : k.corr;
+      const float l1 = sqrtf(dot3a(f1, f1)), l2 = sqrtf(dot3a(f2, f2));
+      const float kk = 2.0f * k.kj * cos_t;
+      const float dp = d_phi32<ROUGH>(a.n_terms, lg, fad, k.fadL, sg, lc, kk,
+                                      2.0f * k.kj * d1 / l1,
+                                      2.0f * k.kj * d2 / l2, l1, l2);
+      const float sk = sg * kk;
+      cr = amp * __expf(-0.5f * sk * sk);
+      if (fa > 0.0f) {
+        const float ai = base * sqrtf(dp);
+        cr += ai * a.F.phasor[2 * i];
+        ci += ai * a.F.phasor[2 * i + 1];
+      }
+    }
+    if (a.F.diffuse_amp && fa > 0.0f) {
+      const float ct = fmaxf(cos_t, 0.0f);
+      const float ad = sqrtf(fa * 0.15915494309f) *
+                       (float)a.F.diffuse_amp[i] * ct *
+                       (ct > 0.0f ? __powf(ct, 0.5f * k.n_exp)
+                                  : (k.n_exp == 0.0f ? 1.0f : 0.0f)) *
+                       spread * att_f;
+      cr += ad * a.F.diffuse_phasor[2 * i];
+      ci += ad * a.F.diffuse_phasor[2 * i + 1];
+    }
+    // carrier phase 2 k0 opl mod 2 pi (double-float, Cody-Waite)
+    float ph, pe;
+    two_prod(k.K2h, opl.hi, ph, pe);
+    const float pl = pe + __fmaf_rn(k.K2h, opl.lo, k.K2l * opl.hi);
+    const float n2 = rintf(ph * 0.159154943091895336f);
+    float red = __fmaf_rn(-n2, 6.28318548202514648f, ph);  // exact
+    red = __fmaf_rn(-n2, -1.74845553146951e-07f, red) + pl;
+    float sn, cs;
+    __sincosf(red, &sn, &cs);
+    re = cr * sn - ci * cs;
+    im = cr * cs + ci * sn;
+    pwr = re * re + im * im;
+  } else {
+    const float aa = fa * cos_t * spread;
+    re = aa * aa * att_f * att_f;
+    im = 0.0f;
+    pwr = re;
+  }
+  // fast-time bin u = opl A - B (double-float), float64 path near edges
+  float up, ue, us, ue2;
+  two_prod(opl.hi, k.Ah, up, ue);
+  two_sum(up, -k.Bh, us, ue2);
+  const float ul = (ue2 + ue) + __fmaf_rn(opl.hi, k.Al, opl.lo * k.Ah) - k.Bl;
+  float fb = floorf(us);
+  float frac = (us - fb) + ul;
+  if (frac < 0.0f) { fb -= 1.0f; frac += 1.0f; }
+  else if (frac >= 1.0f) { fb += 1.0f; frac -= 1.0f; }
+  if ((frac < kBinGuard || frac > 1.0f - kBinGuard) && us > -4.0f &&
+      us < nsf + 4.0f) {
+    if (!EXACT) return false;
+    bool v64;
+    const double q64[3] = {q[0], q[1], q[2]};
+    const double o64 = full_opl64<NI>(a, p64, q64, v64);
+    const double twtt = __ddiv_rn(__dmul_rn(2.0, o64), a.c);
+    fb = (float)floor(__ddiv_rn(__dsub_rn(twtt, a.t0), a.dt));
+  }
+  o.re = re;
+  o.im = im;
+  o.pwr = pwr;
+  o.bin = -1;
+  if (P.valid && fb >= 0.0f && fb < nsf) {
+    int b = (int)fb;
+    if (a.split) {
+      const float v[3] = {q[0] - T.ph[0], q[1] - T.ph[1], q[2] - T.ph[2]};
+      if (dot3a(v, u) > 0.0f) b += a.n_samples;
+    }
+    o.bin = b;
+  }
+  return true;
+}
+
+// Fast kernel: CTA = (facet chunk, trace block); thread <-> facet; per-trace
+// histograms in shared memory; pairs that need a float64 decision are marked
+// in the deferral bitmask (bit t * defer_w + (i - lo_t)).
 template <int NI, int ROUGH>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kSplitThreads)
 refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *hist = reinterpret_cast<float2 *>(smem_raw);
@@ -645,25 +828,11 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   const int t_base = blockIdx.y * a.tb;
   const int nt = min(a.tb, a.T - t_base);
   const int tid = threadIdx.x;
-  int pa_len = 0, pb_len = 0;
-  if (a.pat_kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
-  if (a.pat_kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
-  if (a.pat_kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * a.pat_n; pb_len = 4; }
-  if (a.pat_kind == SS_PAT_TABULATED) { pa_len = a.pat_n; pb_len = a.pat_n; }
+  int pa_len, pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
   if (tid < nt) {
     const int t = t_base + tid;
-    for (int j = 0; j < 3; ++j) {
-      const double pj = a.pos[3 * t + j];
-      s_p64[tid][j] = pj;
-      const df v = df_from_double(pj);
-      s_tr[tid].ph[j] = v.hi;
-      s_tr[tid].pl[j] = v.lo;
-      s_tr[tid].pm0[j] = (float)(pj - a.ifc[0].mean_point[j]);
-      s_u[tid][j] = a.uct ? (float)a.uct[3 * t + j] : 0.0f;
-    }
-    for (int j = 0; j < 6; ++j)
-      s_pv[tid][j] =
-          (a.pv && j < a.pv_len) ? (float)a.pv[a.pv_len * t + j] : 0.0f;
+    load_trace(a, t, s_tr[tid], s_p64[tid], s_u[tid], s_pv[tid]);
     long lo = (long)a.off[t] * a.bs;
     long hi = min((long)(a.off[t] + a.n_win) * a.bs, (long)a.N);
     s_lo[tid] = (int)min(lo, (long)a.N);
@@ -693,130 +862,25 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   }
   __syncthreads();
 
-  const int nj = a.leg_last;
-  const float n0 = k.n_leg[0], njn = k.n_leg[nj];
-  const df njd = df_make(k.n_leg[nj], k.n_leg_lo[nj]);
-  const float nsf = (float)a.n_samples;
   for (int i = s_rng[0] + tid; i < s_rng[1]; i += blockDim.x) {
     const float q[3] = {a.F.cx[i], a.F.cy[i], a.F.cz[i]};
-    const float fn[3] = {a.F.nx[i], a.F.ny[i], a.F.nz[i]};
-    const float fa = a.F.area[i];
     for (int tt = 0; tt < nt; ++tt) {
       if (i < s_lo[tt] || i >= s_hi[tt]) continue;
-      PathS P;
-      if (NI == 0)
-        path_sequential_split(a, k, s_tr[tt], s_p64[tt], q, P);
-      else
-        path_joint_split<NI == 0 ? 1 : NI>(a, k, s_tr[tt], s_p64[tt], q, P);
-      // final leg (medium j)
-      const df opl = df_add(P.opl, df_mul(P.s_last, njd));
-      const float s_j = P.s_last.hi;
-      const float *rh = P.rh;
-      const float loss = P.loss_db + s_j * (k.att_leg[nj] * 1e-3f);
-      const float sperp = P.sum_perp + s_j / njn;
-      const float spar = P.sum_par + s_j / (njn * P.c_last * P.c_last);
-      const float l_perp = n0 * sperp;
-      const float l_par = n0 * P.c0 * P.c0 * spar;
-      const float flux = (n0 * P.c0) / (njn * P.c_last);
-      const float att_f = exp2f(-loss * 0.33219280949f);  // 10^(-loss/10)
-      const float cos_t = dot3a(rh, fn);
-      float spread = P.tau2 * flux / (l_par * l_perp);
-      if (a.pat_kind != SS_PAT_ISOTROPIC) {
-        const float dm = rsqrtf(fmaxf(dot3a(P.d0, P.d0), 1e-30f));
-        const float g = gain32(a.pat_kind, a.pat_n, pa_len, s_pat, s_pv[tt],
-                               P.d0[0] * dm, P.d0[1] * dm, P.d0[2] * dm);
-        spread *= g * g;
+      PairOut o;
+      if (!pair_eval<NI, ROUGH, false>(a, k, s_tr[tt], s_p64[tt], s_u[tt],
+                                       s_pv[tt], s_pat, pa_len, lg, s_fad, i,
+                                       q, o)) {
+        const unsigned long long bit =
+            (unsigned long long)(t_base + tt) * a.defer_w + (i - s_lo[tt]);
+        atomicOr(&a.defer_mask[bit >> 5], 1u << (bit & 31));
+        continue;
       }
-      float re, im, pwr;
-      if (a.coherent) {
-        const float gam = a.F.gamma_f64 ? (float)a.F.gamma_f64[i]
-                                        : (float)a.gamma;
-        const float f1[3] = {a.F.e1x[i], a.F.e1y[i], a.F.e1z[i]};
-        const float f2[3] = {a.F.e2x[i], a.F.e2y[i], a.F.e2z[i]};
-        const float d1 = dot3a(rh, f1), d2 = dot3a(rh, f2);
-        const float base = k.amp_pref_j * gam * cos_t * spread * att_f;
-        float amp = base * fa * sinc32(k.kj * d1) * sinc32(k.kj * d2);
-        if (a.taper) {
-          const float ct = fminf(fmaxf(cos_t, (float)kCMin), 1.0f);
-          const float ct2 = ct * ct;
-          amp *= __expf(-__fdividef(1.0f - ct2, ct2) * k.taper_inv);
-        }
-        float cr = amp, ci = 0.0f;
-        if (ROUGH != SS_ROUGH_NONE) {
-          const float sg = a.F.sigma ? a.F.sigma[i] : k.sigma;
-          const float lc = a.F.corr ? a.F.corr[i] : k.corr;
-          const float l1 = sqrtf(dot3a(f1, f1)), l2 = sqrtf(dot3a(f2, f2));
-          const float kk = 2.0f * k.kj * cos_t;
-          const float dp = d_phi32<ROUGH>(a.n_terms, lg, s_fad, k.fadL, sg, lc,
-                                          kk, 2.0f * k.kj * d1 / l1,
-                                          2.0f * k.kj * d2 / l2, l1, l2);
-          const float sk = sg * kk;
-          cr = amp * __expf(-0.5f * sk * sk);
-          if (fa > 0.0f) {
-            const float ai = base * sqrtf(dp);
-            cr += ai * a.F.phasor[2 * i];
-            ci += ai * a.F.phasor[2 * i + 1];
-          }
-        }
-        if (a.F.diffuse_amp && fa > 0.0f) {
-          const float ct = fmaxf(cos_t, 0.0f);
-          const float ad = sqrtf(fa * 0.15915494309f) *
-                           (float)a.F.diffuse_amp[i] * ct *
-                           (ct > 0.0f ? __powf(ct, 0.5f * k.n_exp)
-                                      : (k.n_exp == 0.0f ? 1.0f : 0.0f)) *
-                           spread * att_f;
-          cr += ad * a.F.diffuse_phasor[2 * i];
-          ci += ad * a.F.diffuse_phasor[2 * i + 1];
-        }
-        // carrier phase 2 k0 opl mod 2 pi (double-float, Cody-Waite)
-        float ph, pe;
-        two_prod(k.K2h, opl.hi, ph, pe);
-        const float pl = pe + __fmaf_rn(k.K2h, opl.lo, k.K2l * opl.hi);
-        const float n2 = rintf(ph * 0.159154943091895336f);
-        float red = __fmaf_rn(-n2, 6.28318548202514648f, ph);  // exact
-        red = __fmaf_rn(-n2, -1.74845553146951e-07f, red) + pl;
-        float sn, cs;
-        __sincosf(red, &sn, &cs);
-        re = cr * sn - ci * cs;
-        im = cr * cs + ci * sn;
-        pwr = re * re + im * im;
+      if (o.bin >= 0) {
+        float2 *h = hist + (size_t)tt * a.n_seg + o.bin;
+        atomicAdd(&h->x, o.re);
+        if (a.coherent) atomicAdd(&h->y, o.im);
       } else {
-        const float aa = fa * cos_t * spread;
-        re = aa * aa * att_f * att_f;
-        im = 0.0f;
-        pwr = re;
-      }
-      // fast-time bin u = opl A - B (double-float), float64 path near edges
-      float up, ue, us, ue2;
-      two_prod(opl.hi, k.Ah, up, ue);
-      two_sum(up, -k.Bh, us, ue2);
-      const float ul = (ue2 + ue) + __fmaf_rn(opl.hi, k.Al, opl.lo * k.Ah) -
-                       k.Bl;
-      float fb = floorf(us);
-      float frac = (us - fb) + ul;
-      if (frac < 0.0f) { fb -= 1.0f; frac += 1.0f; }
-      else if (frac >= 1.0f) { fb += 1.0f; frac -= 1.0f; }
-      if ((frac < kBinGuard || frac > 1.0f - kBinGuard) && us > -4.0f &&
-          us < nsf + 4.0f) {
-        bool v64;
-        const double q64[3] = {q[0], q[1], q[2]};
-        const double o64 = full_opl64<NI>(a, s_p64[tt], q64, v64);
-        const double twtt = __ddiv_rn(__dmul_rn(2.0, o64), a.c);
-        fb = (float)floor(__ddiv_rn(__dsub_rn(twtt, a.t0), a.dt));
-      }
-      const bool ok = P.valid && fb >= 0.0f && fb < nsf;
-      if (ok) {
-        int b = (int)fb;
-        if (a.split) {
-          const float v[3] = {q[0] - s_tr[tt].ph[0], q[1] - s_tr[tt].ph[1],
-                              q[2] - s_tr[tt].ph[2]};
-          if (dot3a(v, s_u[tt]) > 0.0f) b += a.n_samples;
-        }
-        float2 *h = hist + (size_t)tt * a.n_seg + b;
-        atomicAdd(&h->x, re);
-        if (a.coherent) atomicAdd(&h->y, im);
-      } else {
-        atomicAdd(&s_drop[tt], pwr);
+        atomicAdd(&s_drop[tt], o.pwr);
       }
     }
   }
@@ -831,6 +895,98 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
     a.part_drop[(size_t)chunk * a.T + t_base + tid] = (double)s_drop[tid];
 }
 
+// Fix-up kernel: evaluates the deferred pairs with the float64 decisions
+// and adds them to facet chunk 0's partials, which the fast kernel has
+// written in full. Deferred pairs are sparse (a few per thousand bits), so
+// each warp scans 32 mask words at a time and queues their set bits in
+// shared memory, then evaluates them 32 at a time with every lane busy.
+constexpr int kFixWarps = 4;
+constexpr int kFixQueue = 32 * 32 + 32;  // one scan round plus a partial batch
+
+template <int NI, int ROUGH>
+__device__ __forceinline__ void fixup_pair(const RefArgs &a,
+                                           const RefSplitConsts &k,
+                                           unsigned long long bit,
+                                           const float *pat, int pa_len,
+                                           const float *lg, const float *fad) {
+  const int t = (int)(bit / a.defer_w);
+  const long lo = min((long)a.off[t] * a.bs, (long)a.N);
+  const int i = (int)(lo + (long)(bit % a.defer_w));
+  TraceS T;
+  double p64[3];
+  float u[3], pv[6];
+  load_trace(a, t, T, p64, u, pv);
+  const float q[3] = {a.F.cx[i], a.F.cy[i], a.F.cz[i]};
+  PairOut o;
+  pair_eval<NI, ROUGH, true>(a, k, T, p64, u, pv, pat, pa_len, lg, fad, i, q,
+                             o);
+  if (o.bin >= 0) {
+    float2 *h = reinterpret_cast<float2 *>(a.part) + (size_t)t * a.n_seg +
+                o.bin;
+    atomicAdd(&h->x, o.re);
+    if (a.coherent) atomicAdd(&h->y, o.im);
+  } else {
+    atomicAdd(&a.part_drop[t], (double)o.pwr);
+  }
+}
+
+template <int NI, int ROUGH>
+__global__ void __launch_bounds__(32 * kFixWarps)
+refracted_split_fixup(RefArgs a, RefSplitConsts k) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *lg = reinterpret_cast<float *>(smem_raw);
+  __shared__ float s_pat[SS_PAT_MAX];
+  __shared__ float s_fad[SS_FAD_N];
+  __shared__ unsigned long long s_q[kFixWarps][kFixQueue];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  int pa_len, pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
+  for (int j = tid; j < pa_len; j += blockDim.x) s_pat[j] = (float)a.pa[j];
+  for (int j = tid; j < pb_len; j += blockDim.x)
+    s_pat[pa_len + j] = (float)a.pb[j];
+  if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
+    s_fad[tid] = (float)a.fad.a[tid];
+  if (ROUGH != SS_ROUGH_NONE)
+    for (int m = tid; m <= a.n_terms; m += blockDim.x)
+      lg[m] = (float)lgamma((double)m + 1.0);
+  __syncthreads();
+  const unsigned long long n_words =
+      ((unsigned long long)a.T * a.defer_w + 31) >> 5;
+  const unsigned long long n_warps =
+      (unsigned long long)gridDim.x * kFixWarps;
+  unsigned long long *q = s_q[warp];
+  int qn = 0;  // queued bits (warp-uniform)
+  for (unsigned long long base =
+           ((unsigned long long)blockIdx.x * kFixWarps + warp) * 32;
+       base < n_words; base += n_warps * 32) {
+    const unsigned long long w = base + lane;
+    unsigned int m = w < n_words ? a.defer_mask[w] : 0u;
+    const int c = __popc(m);
+    int incl = c;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int pos = qn + incl - c;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      q[pos++] = (w << 5) + b;
+    }
+    __syncwarp();
+    qn += total;
+    while (qn >= 32) {
+      const unsigned long long bit = q[qn - 32 + lane];
+      __syncwarp();
+      fixup_pair<NI, ROUGH>(a, k, bit, s_pat, pa_len, lg, s_fad);
+      qn -= 32;
+    }
+    __syncwarp();
+  }
+  if (lane < qn) fixup_pair<NI, ROUGH>(a, k, q[lane], s_pat, pa_len, lg, s_fad);
+}
+
 template <int NI, int ROUGH>
 static int launch_split(RefArgs &a, const RefSplitConsts &k, const Plan &p,
                         size_t smem, cudaStream_t st) {
@@ -838,9 +994,24 @@ static int launch_split(RefArgs &a, const RefSplitConsts &k, const Plan &p,
       refracted_split_kernel<NI, ROUGH>,
       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return cuda_status(e, "refracted_split smem");
+  const unsigned long long n_words =
+      ((unsigned long long)a.T * a.defer_w + 31) >> 5;
+  e = cudaMemsetAsync(a.defer_mask, 0, n_words * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_status(e, "deferral mask clear");
   dim3 grid(p.n_chunks, p.n_groups);
   refracted_split_kernel<NI, ROUGH><<<grid, p.threads, smem, st>>>(a, k);
-  return cuda_status(cudaGetLastError(), "refracted_split launch");
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "refracted_split launch");
+  const size_t fsmem =
+      a.rough_kind ? (size_t)(a.n_terms + 1) * sizeof(float) : 0;
+  const unsigned long long want = (n_words + 32 * kFixWarps - 1) /
+                                  (32 * kFixWarps);
+  const int blocks =
+      (int)std::max<unsigned long long>(1, std::min<unsigned long long>(
+                                               want, 8ull * sm_count()));
+  refracted_split_fixup<NI, ROUGH><<<blocks, 32 * kFixWarps, fsmem, st>>>(a,
+                                                                          k);
+  return cuda_status(cudaGetLastError(), "refracted_split fix-up launch");
 }
 
 template <int NI>
@@ -857,11 +1028,8 @@ static int launch_split_r(RefArgs &a, const RefSplitConsts &k, const Plan &p,
 }
 
 int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
-  int pa_len = 0, pb_len = 0;
-  if (a.pat_kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
-  if (a.pat_kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
-  if (a.pat_kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * a.pat_n; pb_len = 4; }
-  if (a.pat_kind == SS_PAT_TABULATED) { pa_len = a.pat_n; pb_len = a.pat_n; }
+  int pa_len, pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
   if (pa_len + pb_len > SS_PAT_MAX) {
     set_error("antenna table too large for the split kernel");
     return SS_ERR_UNSUPPORTED;
