@@ -44,6 +44,10 @@ def parse():
                     help="skip the float64-form step and the error check")
     ap.add_argument("--skip-e2e", action="store_true",
                     help="skip the drop-in (host buffers) step")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per launch of the dominant kernel from "
+                         "an ncu capture of the same workload (reported in "
+                         "the roofline object)")
     ap.add_argument("--fp64-traces", type=int, default=256,
                     help="traces of the float64-form step (its rate is per "
                          "pair; the error check covers these traces)")
@@ -286,7 +290,6 @@ def main():
         dist.init_process_group("nccl", device_id=device)
 
     from radar_sounder_simulator_gb300 import scenes
-    from radar_sounder_simulator_gb300.coherent import coherent_run_count
     cfg = scenes.config2(n_cells=args.n_cells, n_traces=args.n_traces,
                          line_offset_y=200.0 * rank)
     pairs_step = sum(len(f.centers) for f in cfg.layers) * len(cfg.pos)
@@ -374,8 +377,11 @@ def main():
         torch.cuda.synchronize()
         e2e_s = time.perf_counter() - t0
 
-    launches = args.steps * sum(coherent_run_count(p) for p in plans)
-    roof = roofline(per_kernel, plans)
+    launches = args.steps * sum(p.kernel_launches() for p in plans)
+    peak = fp32_peak_tflops(device)
+    roof = roofline(per_kernel, [len(f.centers) * len(cfg.pos)
+                                 for f in cfg.layers], peak,
+                    traffic=args.traffic)
     if rank == 0:
         cpu = None
         if ws == 1 and args.cpu_seconds > 0:
@@ -425,12 +431,92 @@ def split_error(outs, outs64):
     return worst
 
 
-def roofline(per_kernel_ms, plans):
-    """Dominant kernel's position against the FP32 pipe (filled in from the
-    per-pair operation counts of the kernel that dominates the step)."""
+# --------------------------------------------------------------------------
+# roofline: algorithmic FLOP per pair and the measured FP32 FMA rate
+# --------------------------------------------------------------------------
+# Floating-point operations per (trace, facet) pair of the reference
+# algorithm at its fixed budgets (an FMA counts 2; sqrt, divide and the
+# transcendental functions count 1 each and are also MUFU work):
+#   * smooth isotropic pair, delta-binned (kernels/coherent.py:107-128 plus
+#     geometry.py:18-24 and the accumulate): 47;
+#   * one sequential crossing (multilayer.py:352-406): 10 + 25 Snell
+#     iterations of 20 (multilayer.py:225-240) plus 60 for the facet lookup,
+#     plane set-up and Fresnel: 760;
+#   * joint path over C crossings, S = C + 1 segments
+#     (multilayer.py:408-457, refraction_joint.py:143-322): mean-plane lookup
+#     chain 260 C, chain initialiser 560 C, six Newton steps of
+#     5 G + 28 S + 61 C + 54 (C - 1) + 58 C + 40 C (one geometry evaluation
+#     G = 25 C + 15 S for the step and four for the step-halving candidates,
+#     the W blocks, the block-tridiagonal assembly and block-Thomas solve),
+#     final polyline 12 S + 80 C;
+#   * final leg, radiometry, amplitude, carrier phase and bin: 25 C + 80.
+def pair_flops(n_crossed, joint):
+    if n_crossed == 0:
+        return 47.0
+    C = n_crossed
+    if not joint:
+        return 760.0 * C + 25.0 * C + 80.0
+    S = C + 1
+    G = 25.0 * C + 15.0 * S
+    newton = 5 * G + 28 * S + 61 * C + 54 * (C - 1) + 58 * C + 40 * C
+    return (260.0 * C + 560.0 * C + 6 * newton + 12 * S + 80 * C +
+            25.0 * C + 80.0)
+
+
+LAYER_PATHS = [(0, False), (1, False), (2, True), (3, True)]
+
+
+def fp32_peak_tflops(device, repeats=5):
+    """FP32 FMA rate of this GPU, measured with the library's probe kernel
+    (best of ``repeats`` launches, TFLOP/s)."""
+    import ctypes as C
+    import torch
+    from radar_sounder_simulator_gb300 import _lib
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    blocks, iters = 8 * sms, 40000
+    out = torch.empty(blocks * 256, dtype=torch.float32, device=device)
+    stream = torch.cuda.current_stream(device)
+    L = _lib.lib()
+
+    def launch():
+        _lib.check(L.ss_fp32_fma_probe(blocks, iters,
+                                       C.c_void_p(out.data_ptr()),
+                                       C.c_void_p(stream.cuda_stream)),
+                   "ss_fp32_fma_probe")
+    for _ in range(3):
+        launch()
+    best = 0.0
+    for _ in range(repeats):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        flop = blocks * 256 * 8 * iters * 2.0
+        best = max(best, flop / (e0.elapsed_time(e1) * 1e-3) / 1e12)
+    return best
+
+
+def roofline(per_kernel_ms, pairs, peak_tflops, traffic=None):
+    """Dominant launch sequence's position against the FP32 pipe."""
     i = int(np.argmax(per_kernel_ms))
     names = ["surface", "h1_seq", "h2_joint", "bed_joint"]
-    return {"kernel": names[i], "ms": per_kernel_ms[i]}
+    kernels = ["coherent_split_kernel", "refracted_split_kernel<0>",
+               "refracted_split_kernel<2>", "refracted_split_kernel<3>"]
+    C, joint = LAYER_PATHS[i]
+    fl = pair_flops(C, joint)
+    achieved = pairs[i] * fl / (per_kernel_ms[i] * 1e-3) / 1e12
+    return {"bound": "fp32", "achieved": achieved, "peak": peak_tflops,
+            "unit": "TFLOP/s", "frac": achieved / peak_tflops,
+            "traffic": traffic, "kernel": kernels[i], "layer": names[i],
+            "flop_per_pair": fl, "pairs_per_launch": pairs[i],
+            "ms_per_launch": per_kernel_ms[i],
+            "peak_source": "FP32 FMA probe (ss_fp32_fma_probe) measured in "
+                           "this run; the measured-peaks file has no FP32 "
+                           "figure",
+            "timed": "main pass + fix-up + chunk reduce of that layer, CUDA "
+                     "events on the launching stream"}
 
 
 if __name__ == "__main__":

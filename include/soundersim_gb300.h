@@ -245,6 +245,14 @@ int ss_refracted_fwd(const ss_refracted_opts *opts, const ss_facets *target,
                      const ss_roughness *rough, const ss_output *out,
                      void *scratch, size_t scratch_bytes, void *stream);
 
+/* FP32 FMA throughput probe (no counterpart in the reference; measurement
+ * helper). Launches `blocks` CTAs of 256 threads, each thread running eight
+ * independent FMA chains of `iters` steps, and writes blocks * 256 floats to
+ * `out`. FLOP per launch = blocks * 256 * 8 * iters * 2; the caller times
+ * the launch on `stream`. */
+int ss_fp32_fma_probe(int32_t blocks, int32_t iters, float *out,
+                      void *stream);
+
 /* Library build string (kernel version, arch) for result provenance. */
 const char *ss_version(void);
 

@@ -102,6 +102,8 @@ SIGNATURES = {
                                    C.POINTER(Pattern), C.POINTER(Roughness),
                                    C.POINTER(Output), C.c_void_p, C.c_size_t,
                                    C.c_void_p]),
+    "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
+                                    C.c_void_p]),
     "ss_version": (C.c_char_p, []),
     "ss_last_error": (C.c_char_p, []),
 }

@@ -160,6 +160,11 @@ class CoherentPlan:
         _lib.check(st, "ss_coherent_fwd")
         return field, dropped
 
+    def kernel_launches(self):
+        """Library kernels one ``run()`` launches (main pass + chunk
+        reduce)."""
+        return 2
+
     def to_numpy(self, field, dropped, out_dtype=np.complex64):
         f = field.cpu().numpy()
         res = (f[..., 0] + 1j * f[..., 1]).astype(out_dtype)
@@ -170,7 +175,7 @@ class CoherentPlan:
 
 def coherent_run_count(plan):
     """Library kernels one ``run()`` launches (main pass + chunk reduce)."""
-    return 2
+    return plan.kernel_launches()
 
 
 def prepare_coherent(positions, u_ct, centers, normals, areas, e1, e2, *, k,

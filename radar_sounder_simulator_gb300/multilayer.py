@@ -92,6 +92,11 @@ class RefractedPlan:
         _lib.check(st, "ss_refracted_fwd")
         return field, dropped
 
+    def kernel_launches(self, precision=None):
+        """Library kernels one ``run()`` launches: main pass and chunk
+        reduce, plus the split form's fix-up pass."""
+        return 2 if (precision or self.precision) == "fp64" else 3
+
     def to_numpy(self, field, dropped, out_dtype=None):
         f = field.cpu().numpy()
         if self.coherent:
