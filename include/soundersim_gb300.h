@@ -245,6 +245,65 @@ int ss_refracted_fwd(const ss_refracted_opts *opts, const ss_facets *target,
                      const ss_roughness *rough, const ss_output *out,
                      void *scratch, size_t scratch_bytes, void *stream);
 
+/* Pulse compression of kernel output along fast time. */
+typedef struct {
+  int32_t n_traces;  /* T */
+  int32_t n_samples; /* B: fast-time samples per trace */
+  int32_t n_lanes;   /* L: trailing lanes, e.g. 2 for split sides (T, B, 2) */
+  int32_t n_taps;    /* pulse length 2M + 1 */
+  int32_t center;    /* index of the pulse's zero lag (M) */
+  int32_t power;     /* 0: complex field with complex taps;
+                        1: real power with real taps (|p|^2), output >= 0 */
+  int32_t in_f64;    /* input elements: 1 = float64, 0 = float32
+                        (complex: interleaved re, im) */
+} ss_waveform_opts;
+
+/* 'same'-mode convolution y[t, i, l] = sum_j taps[j] x[t, i + center - j, l]
+ * of a (T, B, L) array with the compressed pulse; replaces
+ * convolve_fast_time (waveform.py:126-138) as used by apply_waveform
+ * (waveform.py:141-160). taps: device float64, (n_taps, 2) re/im pairs
+ * (power = 0) or (n_taps,) (power = 1). Input is rounded to float32 first
+ * (the reference convolves the kernel's complex64 output); out: float32
+ * (re, im) pairs (power = 0) or float32 clipped at 0 (power = 1). */
+int ss_range_compress(const ss_waveform_opts *opts, const double *taps,
+                      const void *in, void *out, void *stream);
+
+/* Frequency-sampled synthesis (Mode F). */
+typedef struct {
+  double f0;          /* band centre (Hz) */
+  double bandwidth;   /* band width B (Hz) */
+  double c;           /* wave speed (m/s) */
+  double gamma;       /* reflection coefficient (facets->gamma_f32 overrides) */
+  double taper_s;     /* off-specular taper slope (used when taper != 0) */
+  int32_t n_freq;     /* K midpoint samples f_k = f0 - B/2 + (k + 1/2) B/K */
+  int32_t freeze_amplitudes; /* 1: amplitudes at f0, exact phase per f_k */
+  int32_t taper;
+  int32_t block_size; /* per-trace facet windows, as ss_coherent_opts */
+  int32_t n_win;
+  int32_t precision;  /* SS_PREC_FP64 or SS_PREC_SPLIT */
+} ss_multifreq_opts;
+
+size_t ss_multifreq_scratch_bytes(const ss_multifreq_opts *opts,
+                                  int32_t n_traces, int32_t n_facets);
+
+/* Band response H[t, k] = sum over the trace's facet window of the LPA
+ * contribution at f_k (compare/multifreq.py:78-96, lpa_contributions of
+ * kernels/coherent.py:107-128), for every trace. H: device float64
+ * (T, K, 2) re/im. Roughness (frozen amplitudes, split form) uses
+ * facets->sigma/corr/phasor as ss_coherent_fwd does. */
+int ss_multifreq_response(const ss_multifreq_opts *opts,
+                          const ss_facets *facets, const ss_traces *traces,
+                          const ss_roughness *rough, double *H,
+                          void *scratch, size_t scratch_bytes, void *stream);
+
+/* Synthesis y[t, b] = sum_k wbar[k] H[t, k] exp(2j pi (f_k - f0) twtt[b])
+ * (compare/multifreq.py:98). wbar (K,), twtt (B,), y (T, B, 2) float64
+ * device arrays. */
+int ss_multifreq_synth(const ss_multifreq_opts *opts, int32_t n_traces,
+                       const double *H, const double *wbar,
+                       const double *twtt, int32_t n_twtt, double *y,
+                       void *stream);
+
 /* FP32 FMA throughput probe (no counterpart in the reference; measurement
  * helper). Launches `blocks` CTAs of 256 threads, each thread running eight
  * independent FMA chains of `iters` steps, and writes blocks * 256 floats to

@@ -65,3 +65,18 @@ def multifreq_profile(position, centers, normals, areas, e1, e2, *, gamma,
     w = window_weights(freqs, f0, bandwidth, window)
     wbar = w / w.sum()
     return (wbar * H) @ np.exp(2j * np.pi * np.outer(freqs - f0, twtt))
+
+
+def synth_frozen(r, amp0, *, f0, bandwidth, c, twtt, n_freq, window="hann"):
+    """Frozen-amplitude synthesis from per-facet ranges ``r`` and complex
+    amplitudes ``amp0`` (the contribution at f0 with its carrier phase
+    removed): y = sum_k Wbar_k sum_n amp0_n exp(-2j k_k r_n)
+    exp(2j pi (f_k - f0) twtt) (multifreq.py:82-98 with any amplitude
+    model, e.g. the rough-facet field)."""
+    freqs = band_frequencies(f0, bandwidth, n_freq)
+    w = window_weights(freqs, f0, bandwidth, window)
+    wbar = w / w.sum()
+    H = np.array([np.sum(amp0 * np.exp(-2j * (2.0 * np.pi * f / c) * r))
+                  for f in freqs])
+    return (wbar * H) @ np.exp(2j * np.pi * np.outer(freqs - f0,
+                                                     np.asarray(twtt)))

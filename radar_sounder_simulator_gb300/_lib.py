@@ -83,6 +83,21 @@ class RefractedOpts(C.Structure):
 
 
 # entry point name -> (restype, argtypes); the ABI surface the tests check
+class WaveformOpts(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in (
+        "n_traces", "n_samples", "n_lanes", "n_taps", "center", "power",
+        "in_f64")]
+
+
+class MultifreqOpts(C.Structure):
+    _fields_ = [("f0", C.c_double), ("bandwidth", C.c_double),
+                ("c", C.c_double), ("gamma", C.c_double),
+                ("taper_s", C.c_double), ("n_freq", C.c_int32),
+                ("freeze_amplitudes", C.c_int32), ("taper", C.c_int32),
+                ("block_size", C.c_int32), ("n_win", C.c_int32),
+                ("precision", C.c_int32)]
+
+
 SIGNATURES = {
     "ss_coherent_scratch_bytes": (C.c_size_t, [C.POINTER(CoherentOpts),
                                                C.c_int32, C.c_int32]),
@@ -102,6 +117,17 @@ SIGNATURES = {
                                    C.POINTER(Pattern), C.POINTER(Roughness),
                                    C.POINTER(Output), C.c_void_p, C.c_size_t,
                                    C.c_void_p]),
+    "ss_range_compress": (C.c_int, [C.POINTER(WaveformOpts), C.c_void_p,
+                                    C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ss_multifreq_scratch_bytes": (C.c_size_t, [C.POINTER(MultifreqOpts),
+                                                C.c_int32, C.c_int32]),
+    "ss_multifreq_response": (C.c_int, [C.POINTER(MultifreqOpts),
+                                        C.POINTER(Facets), C.POINTER(Traces),
+                                        C.POINTER(Roughness), C.c_void_p,
+                                        C.c_void_p, C.c_size_t, C.c_void_p]),
+    "ss_multifreq_synth": (C.c_int, [C.POINTER(MultifreqOpts), C.c_int32,
+                                     C.c_void_p, C.c_void_p, C.c_void_p,
+                                     C.c_int32, C.c_void_p, C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
     "ss_version": (C.c_char_p, []),
