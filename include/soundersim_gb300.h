@@ -312,6 +312,34 @@ int ss_multifreq_synth(const ss_multifreq_opts *opts, int32_t n_traces,
 int ss_fp32_fma_probe(int32_t blocks, int32_t iters, float *out,
                       void *stream);
 
+/* Adjoint of windowed trace power (no counterpart in the reference). */
+typedef struct {
+  const double *field;       /* (T, n_samples, 2) forward field of the target
+                                (device, the ss_refracted_fwd output) */
+  const double *grad_power;  /* (T,) dL/dP_t, P_t = sum over the window of
+                                |field[t, b]|^2 (device) */
+  int32_t bin_lo, bin_hi;    /* power window [bin_lo, bin_hi) */
+  const double *alpha_mask;  /* host (n_legs,): d att_leg[l] / d alpha */
+  double *grad_gamma_db;     /* (N,) dL/d reflectivity in dB (device) */
+  double *grad_sigma;        /* (N,) dL/d rms height, or NULL (device) */
+  double *grad_alpha;        /* (ss_refracted_adjoint_blocks(N),) partial
+                                sums of dL/d alpha (device; caller adds) */
+} ss_adjoint_io;
+
+int32_t ss_refracted_adjoint_blocks(int32_t n_facets);
+
+/* Gradients of a loss of windowed trace power with respect to per-facet
+ * reflectivity (dB; facets->gamma_f64 holds 10^(R/20)), per-facet
+ * rms height (facets->sigma) and an attenuation rate alpha scaling the legs
+ * of alpha_mask, for the sequential refracted path in coherent mode.
+ * Recomputes every pair (split form with float64 lookup and bin
+ * decisions) -- nothing per pair is stored by the forward. Outputs are in
+ * the facet order of the call. */
+int ss_refracted_adjoint(const ss_refracted_opts *opts,
+                         const ss_facets *target, const ss_traces *traces,
+                         const ss_pattern *pattern, const ss_roughness *rough,
+                         const ss_adjoint_io *io, void *stream);
+
 /* Library build string (kernel version, arch) for result provenance. */
 const char *ss_version(void);
 

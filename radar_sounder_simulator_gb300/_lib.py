@@ -98,6 +98,13 @@ class MultifreqOpts(C.Structure):
                 ("precision", C.c_int32)]
 
 
+class AdjointIO(C.Structure):
+    _fields_ = [("field", C.c_void_p), ("grad_power", C.c_void_p),
+                ("bin_lo", C.c_int32), ("bin_hi", C.c_int32),
+                ("alpha_mask", C.c_void_p), ("grad_gamma_db", C.c_void_p),
+                ("grad_sigma", C.c_void_p), ("grad_alpha", C.c_void_p)]
+
+
 SIGNATURES = {
     "ss_coherent_scratch_bytes": (C.c_size_t, [C.POINTER(CoherentOpts),
                                                C.c_int32, C.c_int32]),
@@ -128,6 +135,12 @@ SIGNATURES = {
     "ss_multifreq_synth": (C.c_int, [C.POINTER(MultifreqOpts), C.c_int32,
                                      C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_int32, C.c_void_p, C.c_void_p]),
+    "ss_refracted_adjoint_blocks": (C.c_int32, [C.c_int32]),
+    "ss_refracted_adjoint": (C.c_int, [C.POINTER(RefractedOpts),
+                                       C.POINTER(Facets), C.POINTER(Traces),
+                                       C.POINTER(Pattern),
+                                       C.POINTER(Roughness),
+                                       C.POINTER(AdjointIO), C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
     "ss_version": (C.c_char_p, []),

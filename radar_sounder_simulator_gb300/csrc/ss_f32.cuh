@@ -201,4 +201,47 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
   return fmaxf(acc, 0.0f);
 }
 
+// D_Phi and its derivative with respect to x = (sigma K)^2 (adjoint): each
+// series term P_m(x) W_m has d/dx = P_m W_m (m / x - 1), so
+// dD/dx = (sum_m m P_m W_m) / x - D.
+template <int KIND>
+__device__ __forceinline__ float d_phi32_dx(int n_terms, const float *lg,
+                                            const float *fa, float fL,
+                                            float sigma, float l, float K,
+                                            float A0, float B0, float Lx,
+                                            float Ly, float &dDdx) {
+  dDdx = 0.0f;
+  const float sk = sigma * K;
+  const float x = sk * sk;
+  if (!(x > 0.0f)) return 0.0f;
+  const float logx = __logf(x);
+  const float kb2 = A0 * A0 + B0 * B0;
+  float acc = 0.0f, accm = 0.0f;
+  for (int m = 1; m <= n_terms; ++m) {
+    const float mf = (float)m;
+    const float im = __fdividef(1.0f, mf);
+    const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
+    float t;
+    if (KIND == SS_ROUGH_GAUSS_AREA) {
+      t = __expf(e - 0.25f * kb2 * l * l * im) *
+          (3.14159265359f * l * l * Lx * Ly * im);
+    } else if (KIND == SS_ROUGH_EXP_AREA) {
+      const float rs = rsqrtf(__fmaf_rn(kb2 * l * l, im * im, 1.0f));
+      t = __expf(e) * (6.28318530718f * l * l * Lx * Ly * im * im) * rs *
+          rs * rs;
+    } else {
+      const float w = __expf(e);
+      t = w == 0.0f ? 0.0f
+                    : w * ((l * l) * (l * l) * im * im) *
+                          f_factor32(fa, fL, mf, A0, Lx, l) *
+                          f_factor32(fa, fL, mf, B0, Ly, l);
+    }
+    acc += t;
+    accm = __fmaf_rn(mf, t, accm);
+  }
+  if (!(acc > 0.0f)) return 0.0f;
+  dDdx = accm / x - acc;
+  return acc;
+}
+
 }  // namespace ss

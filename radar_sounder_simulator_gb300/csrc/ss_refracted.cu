@@ -253,22 +253,24 @@ extern "C" size_t ss_refracted_scratch_bytes(const ss_refracted_opts *opts,
   return ss::refracted_scratch(opts, n_traces, n_facets);
 }
 
-extern "C" int ss_refracted_fwd(const ss_refracted_opts *opts,
-                                const ss_facets *target,
-                                const ss_traces *traces,
-                                const ss_pattern *pattern,
-                                const ss_roughness *rough,
-                                const ss_output *out, void *scratch,
-                                size_t scratch_bytes, void *stream) {
-  using namespace ss;
-  if (!opts || !target || !traces || !out || !opts->crossed ||
+namespace ss {
+
+// Validate the call and fill the argument block shared by the forward and
+// adjoint entry points (everything but the scratch layout).
+static int build_ref_args(const ss_refracted_opts *opts,
+                          const ss_facets *target, const ss_traces *traces,
+                          const ss_pattern *pattern, const ss_roughness *rough,
+                          bool need_output, const ss_output *out, Plan &p,
+                          RefArgs &a) {
+  if (!opts || !target || !traces || (need_output && !out) || !opts->crossed ||
       !opts->n_leg || !opts->eps_leg || !opts->att_leg) {
     set_error("null argument");
     return SS_ERR_ARG;
   }
   const int T = traces->n_traces, N = target->n_facets;
   if (!traces->pos || !traces->off || !target->cx || !target->area ||
-      !out->dropped || (!out->field_c128 && !out->field_c64)) {
+      (need_output &&
+       (!out->dropped || (!out->field_c128 && !out->field_c64)))) {
     set_error("missing required device pointer");
     return SS_ERR_ARG;
   }
@@ -276,7 +278,6 @@ extern "C" int ss_refracted_fwd(const ss_refracted_opts *opts,
     set_error("split_sides needs u_ct");
     return SS_ERR_ARG;
   }
-  Plan p;
   int s = refracted_plan(opts, T, N, &p);
   if (s) {
     set_error(s == SS_ERR_UNSUPPORTED ? "n_samples too large" :
@@ -287,12 +288,7 @@ extern "C" int ss_refracted_fwd(const ss_refracted_opts *opts,
     set_error("k_pad out of range");
     return SS_ERR_ARG;
   }
-  const size_t need = refracted_scratch(opts, T, N);
-  if (!scratch || scratch_bytes < need) {
-    set_error("scratch buffer too small");
-    return SS_ERR_SCRATCH;
-  }
-  RefArgs a{};
+  a = RefArgs{};
   a.F = *target;
   a.pos = traces->pos;
   a.uct = traces->uct;
@@ -368,6 +364,32 @@ extern "C" int ss_refracted_fwd(const ss_refracted_opts *opts,
               "coherent mode");
     return SS_ERR_ARG;
   }
+  a.tb = p.tb;
+  a.n_chunks = p.n_chunks;
+  return SS_OK;
+}
+
+}  // namespace ss
+
+extern "C" int ss_refracted_fwd(const ss_refracted_opts *opts,
+                                const ss_facets *target,
+                                const ss_traces *traces,
+                                const ss_pattern *pattern,
+                                const ss_roughness *rough,
+                                const ss_output *out, void *scratch,
+                                size_t scratch_bytes, void *stream) {
+  using namespace ss;
+  Plan p;
+  RefArgs a;
+  int s = build_ref_args(opts, target, traces, pattern, rough, true, out, p,
+                         a);
+  if (s) return s;
+  const int T = traces->n_traces, N = target->n_facets;
+  const size_t need = refracted_scratch(opts, T, N);
+  if (!scratch || scratch_bytes < need) {
+    set_error("scratch buffer too small");
+    return SS_ERR_SCRATCH;
+  }
   a.part = scratch;
   size_t hist = (size_t)p.n_chunks * T * a.n_seg *
                 (opts->precision == SS_PREC_FP64 ? 16 : 8);
@@ -405,4 +427,39 @@ extern "C" int ss_refracted_fwd(const ss_refracted_opts *opts,
   ReduceArgs r{a.T, a.n_seg, a.n_samples, a.split, a.n_chunks, a.part,
                a.part_drop};
   return launch_reduce(r, opts->precision == SS_PREC_FP64, out, st);
+}
+
+extern "C" int32_t ss_refracted_adjoint_blocks(int32_t n_facets) {
+  return n_facets > 0 ? ss::refracted_adjoint_blocks(n_facets) : 0;
+}
+
+extern "C" int ss_refracted_adjoint(const ss_refracted_opts *opts,
+                                    const ss_facets *target,
+                                    const ss_traces *traces,
+                                    const ss_pattern *pattern,
+                                    const ss_roughness *rough,
+                                    const ss_adjoint_io *io, void *stream) {
+  using namespace ss;
+  if (!io || !io->field || !io->grad_power || !io->grad_gamma_db ||
+      !io->grad_alpha) {
+    set_error("null adjoint argument");
+    return SS_ERR_ARG;
+  }
+  Plan p;
+  RefArgs a;
+  int s = build_ref_args(opts, target, traces, pattern, rough, false, nullptr,
+                         p, a);
+  if (s) return s;
+  if (io->bin_lo < 0 || io->bin_hi > a.n_seg || io->bin_lo >= io->bin_hi) {
+    set_error("power window outside [0, n_samples)");
+    return SS_ERR_ARG;
+  }
+  if (io->grad_sigma && !target->sigma) {
+    set_error("sigma gradients need per-facet rms heights (facets->sigma)");
+    return SS_ERR_ARG;
+  }
+  AdjArgs j{io->field, io->grad_power, io->bin_lo, io->bin_hi,
+            io->grad_gamma_db, io->grad_sigma, io->grad_alpha};
+  return refracted_adjoint_launch(a, j, io->alpha_mask,
+                                  static_cast<cudaStream_t>(stream));
 }

@@ -38,4 +38,18 @@ constexpr int kSplitThreads = 512;
 
 int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st);
 
+// Adjoint inputs and outputs (see ss_refracted_adjoint).
+struct AdjArgs {
+  const double *field;       // (T, n_seg, 2) forward field
+  const double *grad_power;  // (T,) dL/dP_t
+  int bin_lo, bin_hi;        // power window [bin_lo, bin_hi)
+  double *grad_gamma_db;     // (N,)
+  double *grad_sigma;        // (N,) or null
+  double *grad_alpha;        // (refracted_adjoint_blocks(N),) partials
+};
+
+int refracted_adjoint_blocks(int N);
+int refracted_adjoint_launch(RefArgs &a, const AdjArgs &j,
+                             const double *alpha_mask, cudaStream_t st);
+
 }  // namespace ss

@@ -60,6 +60,9 @@ struct RefSplitConsts {
   float n_leg[SS_MAX_IFACE + 1], n_leg_lo[SS_MAX_IFACE + 1],
       eps_leg[SS_MAX_IFACE + 1], att_leg[SS_MAX_IFACE + 1],
       sig_c[SS_MAX_IFACE];
+  // d att_leg / d alpha per leg (adjoint only): the legs whose attenuation
+  // rate is the differentiated parameter
+  float att_mask[SS_MAX_IFACE + 1];
   MeanPlane32 mean[SS_MAX_IFACE];
 };
 
@@ -236,6 +239,7 @@ struct PathS {
   float rh[3];         // unit vector facet -> last crossing
   float d0[3];         // platform -> first crossing
   float loss_db, sum_par, sum_perp, tau2, c0, c_last;
+  float dloss;         // d loss_db / d alpha over these legs (GRAD only)
   bool valid;
   bool defer;          // needs the float64 lookup chain (EXACT = false only)
 };
@@ -253,7 +257,7 @@ __device__ __forceinline__ void p_minus(const TraceS &T, const float *o,
 // ---------------------------------------------------------------------
 // sequential chain (multilayer.py:352-406)
 // ---------------------------------------------------------------------
-template <bool EXACT>
+template <bool EXACT, bool GRAD = false>
 __device__ void path_sequential_split(const RefArgs &a,
                                       const RefSplitConsts &k,
                                       const TraceS &T, const double *p64,
@@ -265,6 +269,7 @@ __device__ void path_sequential_split(const RefArgs &a,
   P.defer = false;
   P.opl = df_make(0.0f, 0.0f);
   P.loss_db = P.sum_par = P.sum_perp = 0.0f;
+  P.dloss = 0.0f;
   P.tau2 = 1.0f;
   P.c0 = P.c_last = 1.0f;
   for (int i = 0; i < a.ni; ++i) {
@@ -323,6 +328,7 @@ __device__ void path_sequential_split(const RefArgs &a,
     }
     const float s1f = s1.hi;
     P.loss_db += s1f * (k.att_leg[i] * 1e-3f);
+    if (GRAD) P.dloss += s1f * (k.att_mask[i] * 1e-3f);
     P.sum_perp += s1f / k.n_leg[i];
     P.sum_par += s1f / (k.n_leg[i] * c_inc * c_inc);
     P.c_last = fmaxf(S.c2, (float)kCMin);
@@ -678,15 +684,24 @@ struct PairOut {
 // guard band of a rounding boundary. The fast kernel holds no float64 code
 // (which halves its registers) and leaves those pairs -- a few per thousand
 // -- to the fix-up kernel, which evaluates them with EXACT = true.
-template <int NI, int ROUGH, bool EXACT>
+// Partial derivatives of one pair's contribution (adjoint only): the part
+// proportional to the facet's reflection coefficient, its derivative with
+// respect to the facet's rms height, and d loss_db / d alpha.
+struct PairGrad {
+  float gre, gim;  // contribution of the gamma-proportional terms
+  float sre, sim;  // d contribution / d sigma
+  float dloss;
+};
+
+template <int NI, int ROUGH, bool EXACT, bool GRAD = false>
 __device__ __forceinline__ bool pair_eval(
     const RefArgs &a, const RefSplitConsts &k, const TraceS &T,
     const double *p64, const float *u, const float *pv, const float *pat,
     int pa_len, const float *lg, const float *fad, int i, const float *q,
-    PairOut &o) {
+    PairOut &o, PairGrad *pg = nullptr) {
   PathS P;
   if (NI == 0)
-    path_sequential_split<EXACT>(a, k, T, p64, q, P);
+    path_sequential_split<EXACT, GRAD>(a, k, T, p64, q, P);
   else
     path_joint_split<NI == 0 ? 1 : NI, EXACT>(a, k, T, p64, q, P);
   if (!EXACT && P.defer) return false;
@@ -730,22 +745,38 @@ __device__ __forceinline__ bool pair_eval(
       amp *= __expf(-__fdividef(1.0f - ct2, ct2) * k.taper_inv);
     }
     float cr = amp, ci = 0.0f;
+    float dcr = 0.0f, dci = 0.0f;  // d (cr, ci) / d sigma (GRAD)
     if (ROUGH != SS_ROUGH_NONE) {
       const float sg = a.F.sigma ? a.F.sigma[i] : k.sigma;
       const float lc = a.F.corr ? a.F.corr[i] : k.corr;
       const float l1 = sqrtf(dot3a(f1, f1)), l2 = sqrtf(dot3a(f2, f2));
       const float kk = 2.0f * k.kj * cos_t;
-      const float dp = d_phi32<ROUGH>(a.n_terms, lg, fad, k.fadL, sg, lc, kk,
-                                      2.0f * k.kj * d1 / l1,
-                                      2.0f * k.kj * d2 / l2, l1, l2);
+      float dpdx = 0.0f;
+      const float dp =
+          GRAD ? d_phi32_dx<ROUGH>(a.n_terms, lg, fad, k.fadL, sg, lc, kk,
+                                   2.0f * k.kj * d1 / l1,
+                                   2.0f * k.kj * d2 / l2, l1, l2, dpdx)
+               : d_phi32<ROUGH>(a.n_terms, lg, fad, k.fadL, sg, lc, kk,
+                                2.0f * k.kj * d1 / l1, 2.0f * k.kj * d2 / l2,
+                                l1, l2);
       const float sk = sg * kk;
-      cr = amp * __expf(-0.5f * sk * sk);
+      const float att_r = __expf(-0.5f * sk * sk);
+      cr = amp * att_r;
+      if (GRAD) dcr = -amp * att_r * sg * kk * kk;
       if (fa > 0.0f) {
-        const float ai = base * sqrtf(dp);
+        const float sq = sqrtf(dp);
+        const float ai = base * sq;
         cr += ai * a.F.phasor[2 * i];
         ci += ai * a.F.phasor[2 * i + 1];
+        if (GRAD && sq > 0.0f) {
+          // d sqrt(D) / d sigma = D'(x) 2 sigma K^2 / (2 sqrt(D))
+          const float dai = base * dpdx * sg * kk * kk / sq;
+          dcr += dai * a.F.phasor[2 * i];
+          dci = dai * a.F.phasor[2 * i + 1];
+        }
       }
     }
+    const float gcr = cr, gci = ci;  // gamma-proportional part
     if (a.F.diffuse_amp && fa > 0.0f) {
       const float ct = fmaxf(cos_t, 0.0f);
       const float ad = sqrtf(fa * 0.15915494309f) *
@@ -768,6 +799,13 @@ __device__ __forceinline__ bool pair_eval(
     re = cr * sn - ci * cs;
     im = cr * cs + ci * sn;
     pwr = re * re + im * im;
+    if (GRAD) {
+      pg->gre = gcr * sn - gci * cs;
+      pg->gim = gcr * cs + gci * sn;
+      pg->sre = dcr * sn - dci * cs;
+      pg->sim = dcr * cs + dci * sn;
+      pg->dloss = P.dloss + s_j * (k.att_mask[nj] * 1e-3f);
+    }
   } else {
     const float aa = fa * cos_t * spread;
     re = aa * aa * att_f * att_f;
@@ -987,6 +1025,153 @@ refracted_split_fixup(RefArgs a, RefSplitConsts k) {
   if (lane < qn) fixup_pair<NI, ROUGH>(a, k, q[lane], s_pat, pa_len, lg, s_fad);
 }
 
+// ---------------------------------------------------------------------
+// adjoint: gradients of windowed trace power
+// ---------------------------------------------------------------------
+// For P_t = sum_{b in [bin_lo, bin_hi)} |F_t[b]|^2 of one target's field F
+// and an upstream gradient g_t = dL/dP_t, a parameter theta of facet i gets
+//   dL/dtheta = sum_t g_t 2 Re(conj(F_t[b_ti]) dc_ti/dtheta)
+// over the pairs whose bin lies in the window (bins and paths do not depend
+// on reflectivity, roughness or attenuation). Each pair's contribution c_ti
+// is recomputed from the geometry -- no per-pair state is stored -- with the
+// float64 lookup and bin decisions (EXACT), so the adjoint sees exactly the
+// forward's pairs. Thread <-> facet, loop over all traces (staged in shared
+// memory in blocks), so each facet's gradient is summed by one thread in
+// trace order; the attenuation-rate gradient is reduced per CTA.
+constexpr int kAdjThreads = 128, kAdjTB = 32;
+
+static RefSplitConsts split_consts(const RefArgs &a);
+
+template <int ROUGH>
+__global__ void __launch_bounds__(kAdjThreads)
+refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *lg = reinterpret_cast<float *>(smem_raw);
+  __shared__ double s_p64[kAdjTB][3];
+  __shared__ TraceS s_tr[kAdjTB];
+  __shared__ float s_u[kAdjTB][3], s_pv[kAdjTB][6];
+  __shared__ int s_lo[kAdjTB], s_hi[kAdjTB];
+  __shared__ double s_g[kAdjTB];
+  __shared__ float s_pat[SS_PAT_MAX];
+  __shared__ float s_fad[SS_FAD_N];
+  __shared__ double s_red[kAdjThreads / 32];
+  const int tid = threadIdx.x;
+  const int i = blockIdx.x * kAdjThreads + tid;
+  const int i_first = blockIdx.x * kAdjThreads;
+  const int i_last = min(i_first + kAdjThreads, a.N) - 1;
+  int pa_len, pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
+  for (int m = tid; m < pa_len; m += blockDim.x) s_pat[m] = (float)a.pa[m];
+  for (int m = tid; m < pb_len; m += blockDim.x)
+    s_pat[pa_len + m] = (float)a.pb[m];
+  if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
+    s_fad[tid] = (float)a.fad.a[tid];
+  if (ROUGH != SS_ROUGH_NONE)
+    for (int m = tid; m <= a.n_terms; m += blockDim.x)
+      lg[m] = (float)lgamma((double)m + 1.0);
+  float q[3] = {0.0f, 0.0f, 0.0f};
+  if (i < a.N) {
+    q[0] = a.F.cx[i];
+    q[1] = a.F.cy[i];
+    q[2] = a.F.cz[i];
+  }
+  double gR = 0.0, gS = 0.0, gA = 0.0;
+  const double2 *F = reinterpret_cast<const double2 *>(j.field);
+  for (int t0 = 0; t0 < a.T; t0 += kAdjTB) {
+    const int nt = min(kAdjTB, a.T - t0);
+    __syncthreads();
+    if (tid < nt) {
+      const int t = t0 + tid;
+      load_trace(a, t, s_tr[tid], s_p64[tid], s_u[tid], s_pv[tid]);
+      const long lo = (long)a.off[t] * a.bs;
+      const long hi = min((long)(a.off[t] + a.n_win) * a.bs, (long)a.N);
+      s_lo[tid] = (int)min(lo, (long)a.N);
+      s_hi[tid] = (int)hi;
+      s_g[tid] = 2.0 * j.grad_power[t];
+    }
+    __syncthreads();
+    for (int tt = 0; tt < nt; ++tt) {
+      // CTA-uniform skip of traces whose window misses the CTA's facets
+      if (s_hi[tt] <= i_first || s_lo[tt] > i_last || s_g[tt] == 0.0)
+        continue;
+      if (i >= a.N || i < s_lo[tt] || i >= s_hi[tt]) continue;
+      PairOut o;
+      PairGrad pg;
+      pair_eval<0, ROUGH, true, true>(a, k, s_tr[tt], s_p64[tt], s_u[tt],
+                                      s_pv[tt], s_pat, pa_len, lg, s_fad, i,
+                                      q, o, &pg);
+      if (o.bin < j.bin_lo || o.bin >= j.bin_hi) continue;
+      const double2 f = F[(size_t)(t0 + tt) * a.n_seg + o.bin];
+      const double g = s_g[tt];
+      gR += g * (f.x * pg.gre + f.y * pg.gim);
+      gS += g * (f.x * pg.sre + f.y * pg.sim);
+      gA += g * (f.x * o.re + f.y * o.im) * (double)pg.dloss;
+    }
+  }
+  // d c / d gamma_dB = c ln(10) / 20; d c / d alpha = -c ln(10) / 10 dloss
+  const double ln10 = 2.302585092994045684;
+  if (i < a.N) {
+    j.grad_gamma_db[i] = gR * (ln10 / 20.0);
+    if (j.grad_sigma) j.grad_sigma[i] = gS;
+  }
+  gA *= -ln10 / 10.0;
+  for (int d = 16; d > 0; d >>= 1) gA += __shfl_down_sync(0xffffffffu, gA, d);
+  if ((tid & 31) == 0) s_red[tid >> 5] = gA;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0.0;
+    for (int w = 0; w < kAdjThreads / 32; ++w) s += s_red[w];
+    j.grad_alpha[blockIdx.x] = s;
+  }
+}
+
+int refracted_adjoint_blocks(int N) {
+  return (N + kAdjThreads - 1) / kAdjThreads;
+}
+
+int refracted_adjoint_launch(RefArgs &a, const AdjArgs &j,
+                             const double *alpha_mask, cudaStream_t st) {
+  int pa_len, pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
+  if (pa_len + pb_len > SS_PAT_MAX) {
+    set_error("antenna table too large for the split kernel");
+    return SS_ERR_UNSUPPORTED;
+  }
+  if (a.joint) {
+    set_error("the adjoint follows the sequential path only");
+    return SS_ERR_UNSUPPORTED;
+  }
+  if (!a.coherent || a.split) {
+    set_error("the adjoint needs coherent mode without split sides");
+    return SS_ERR_UNSUPPORTED;
+  }
+  RefSplitConsts k = split_consts(a);
+  for (int m = 0; m <= a.leg_last; ++m)
+    k.att_mask[m] = alpha_mask ? (float)alpha_mask[m] : 0.0f;
+  const size_t smem =
+      a.rough_kind ? (size_t)(a.n_terms + 1) * sizeof(float) : 0;
+  const int blocks = refracted_adjoint_blocks(a.N);
+  switch (a.rough_kind) {
+    case SS_ROUGH_NONE:
+      refracted_adjoint_kernel<SS_ROUGH_NONE>
+          <<<blocks, kAdjThreads, smem, st>>>(a, k, j);
+      break;
+    case SS_ROUGH_GAUSS_FULL:
+      refracted_adjoint_kernel<SS_ROUGH_GAUSS_FULL>
+          <<<blocks, kAdjThreads, smem, st>>>(a, k, j);
+      break;
+    case SS_ROUGH_GAUSS_AREA:
+      refracted_adjoint_kernel<SS_ROUGH_GAUSS_AREA>
+          <<<blocks, kAdjThreads, smem, st>>>(a, k, j);
+      break;
+    default:
+      refracted_adjoint_kernel<SS_ROUGH_EXP_AREA>
+          <<<blocks, kAdjThreads, smem, st>>>(a, k, j);
+      break;
+  }
+  return cuda_status(cudaGetLastError(), "refracted adjoint launch");
+}
+
 template <int NI, int ROUGH>
 static int launch_split(RefArgs &a, const RefSplitConsts &k, const Plan &p,
                         size_t smem, cudaStream_t st) {
@@ -1027,18 +1212,8 @@ static int launch_split_r(RefArgs &a, const RefSplitConsts &k, const Plan &p,
   }
 }
 
-int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
-  int pa_len, pb_len;
-  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
-  if (pa_len + pb_len > SS_PAT_MAX) {
-    set_error("antenna table too large for the split kernel");
-    return SS_ERR_UNSUPPORTED;
-  }
-  if (a.joint && a.ni > 4) {
-    set_error("split precision joint solve supports up to 4 interfaces; "
-              "use precision='fp64'");
-    return SS_ERR_UNSUPPORTED;
-  }
+// float32 / double-float constants of the split kernels.
+static RefSplitConsts split_consts(const RefArgs &a) {
   RefSplitConsts k{};
   k.k0 = (float)a.k0;
   const double kj = a.k0 * a.n_leg[a.leg_last];
@@ -1088,6 +1263,22 @@ int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
       M.rbl[c] = r.lo;
     }
   }
+  return k;
+}
+
+int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
+  int pa_len, pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
+  if (pa_len + pb_len > SS_PAT_MAX) {
+    set_error("antenna table too large for the split kernel");
+    return SS_ERR_UNSUPPORTED;
+  }
+  if (a.joint && a.ni > 4) {
+    set_error("split precision joint solve supports up to 4 interfaces; "
+              "use precision='fp64'");
+    return SS_ERR_UNSUPPORTED;
+  }
+  const RefSplitConsts k = split_consts(a);
   const size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2) +
                       (a.rough_kind ? (a.n_terms + 1) * sizeof(float) : 0);
   if (!a.joint) return launch_split_r<0>(a, k, p, smem, st);

@@ -238,7 +238,8 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
         T=T, N=n, n_samples=int(n_samples),
         n_seg=int(n_samples) * (2 if split_sides else 1),
         split=bool(split_sides), coherent=coherent, device=device,
-        precision=precision, scratch=None, cull=plan)
+        precision=precision, scratch=None, cull=plan, fac=fac, legs=legs,
+        ifaces=arr)
 
 
 def refracted_cluttergram(positions, u_ct, target, crossed, eps_leg, att_leg,
