@@ -245,6 +245,52 @@ int ss_refracted_fwd(const ss_refracted_opts *opts, const ss_facets *target,
                      const ss_roughness *rough, const ss_output *out,
                      void *scratch, size_t scratch_bytes, void *stream);
 
+/* Batched surface coherent sums (no counterpart in the reference, which
+ * calls coherent_cluttergram once per scene): one job per call of
+ * ss_coherent_fwd, all jobs of a batch with the same precision and
+ * roughness kind. */
+typedef struct {
+  ss_coherent_opts opts;
+  ss_facets facets;
+  ss_traces traces;
+  ss_pattern pattern;   /* kind SS_PAT_ISOTROPIC for none */
+  ss_roughness rough;   /* kind SS_ROUGH_NONE for none */
+  ss_output out;
+} ss_coherent_job;
+
+/* Work decomposition of a batch (0 = default). */
+typedef struct {
+  int32_t threads;       /* CTA size: 128 or 256 (default 256) */
+  int32_t max_tb;        /* traces per work item, 1..8 (default 8) */
+  int32_t items_per_sm;  /* work items per SM; sets facet-chunk sizes
+                            (default 16) */
+  int32_t ctas_per_sm;   /* persistent CTAs per SM (default: as many as fit) */
+} ss_batch_tuning;
+
+/* Filled by ss_coherent_batch_prepare; passed back to ss_coherent_batch_run. */
+typedef struct {
+  int32_t n_jobs, precision, rough_kind, threads, ctas, reserved;
+  int64_t n_items, n_out;
+  uint64_t smem, table_offset;
+} ss_batch_info;
+
+size_t ss_coherent_batch_scratch_bytes(const ss_coherent_job *jobs,
+                                       int32_t n_jobs,
+                                       const ss_batch_tuning *tune);
+
+/* Validates every job, lays out `scratch` (work-queue counter, job table,
+ * per-job partials) and uploads the job table (synchronous). The jobs'
+ * device pointers must stay valid while the batch is run. */
+int ss_coherent_batch_prepare(const ss_coherent_job *jobs, int32_t n_jobs,
+                              const ss_batch_tuning *tune, void *scratch,
+                              size_t scratch_bytes, ss_batch_info *info);
+
+/* Runs a prepared batch on `stream`: one persistent work-queue kernel over
+ * every job's (trace block x facet chunk) items, then one batched reduce
+ * into every job's output. Stream operations only (graph-capturable). */
+int ss_coherent_batch_run(const ss_batch_info *info, void *scratch,
+                          void *stream);
+
 /* Pulse compression of kernel output along fast time. */
 typedef struct {
   int32_t n_traces;  /* T */

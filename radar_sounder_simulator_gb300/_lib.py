@@ -105,6 +105,25 @@ class AdjointIO(C.Structure):
                 ("grad_sigma", C.c_void_p), ("grad_alpha", C.c_void_p)]
 
 
+class CoherentJob(C.Structure):
+    _fields_ = [("opts", CoherentOpts), ("facets", Facets),
+                ("traces", Traces), ("pattern", Pattern),
+                ("rough", Roughness), ("out", Output)]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [("threads", C.c_int32), ("max_tb", C.c_int32),
+                ("items_per_sm", C.c_int32), ("ctas_per_sm", C.c_int32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("n_jobs", C.c_int32), ("precision", C.c_int32),
+                ("rough_kind", C.c_int32), ("threads", C.c_int32),
+                ("ctas", C.c_int32), ("reserved", C.c_int32),
+                ("n_items", C.c_int64), ("n_out", C.c_int64),
+                ("smem", C.c_uint64), ("table_offset", C.c_uint64)]
+
+
 SIGNATURES = {
     "ss_coherent_scratch_bytes": (C.c_size_t, [C.POINTER(CoherentOpts),
                                                C.c_int32, C.c_int32]),
@@ -141,6 +160,13 @@ SIGNATURES = {
                                        C.POINTER(Pattern),
                                        C.POINTER(Roughness),
                                        C.POINTER(AdjointIO), C.c_void_p]),
+    "ss_coherent_batch_scratch_bytes": (C.c_size_t, [
+        C.POINTER(CoherentJob), C.c_int32, C.POINTER(BatchTuning)]),
+    "ss_coherent_batch_prepare": (C.c_int, [
+        C.POINTER(CoherentJob), C.c_int32, C.POINTER(BatchTuning),
+        C.c_void_p, C.c_size_t, C.POINTER(BatchInfo)]),
+    "ss_coherent_batch_run": (C.c_int, [C.POINTER(BatchInfo), C.c_void_p,
+                                        C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
     "ss_version": (C.c_char_p, []),

@@ -24,9 +24,11 @@ namespace ss {
 // ---------------------------------------------------------------------
 // float64 pair evaluation (coherent.py:107-168 + :216-236)
 // ---------------------------------------------------------------------
-__global__ void __launch_bounds__(256)
-coherent_fp64_kernel(CoArgs a) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+// One CTA's work item (facet chunk `chunk` of trace block `group`); shared
+// by the one-call kernel and the batched persistent kernel.
+__device__ __forceinline__ void coherent_fp64_cta(const CoArgs &a, int chunk,
+                                                  int group,
+                                  unsigned char *smem_raw) {
   double2 *hist = reinterpret_cast<double2 *>(smem_raw);
   double *lgam = reinterpret_cast<double *>(hist + (size_t)a.tb * a.n_seg);
   __shared__ double s_p[SS_MAX_TB][3];
@@ -36,8 +38,7 @@ coherent_fp64_kernel(CoArgs a) {
   __shared__ double s_drop[SS_MAX_TB];
   __shared__ int s_rng[2];
 
-  const int chunk = blockIdx.x;
-  const int t_base = blockIdx.y * a.tb;
+  const int t_base = group * a.tb;
   const int nt = min(a.tb, a.T - t_base);
   const int tid = threadIdx.x;
 
@@ -173,6 +174,59 @@ coherent_fp64_kernel(CoArgs a) {
   if (tid < nt) a.part_drop[(size_t)chunk * a.T + t_base + tid] = s_drop[tid];
 }
 
+__global__ void __launch_bounds__(256)
+coherent_fp64_kernel(CoArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  coherent_fp64_cta(a, blockIdx.x, blockIdx.y, smem_raw);
+}
+
+// Batched persistent form (see coherent_batch_split_kernel).
+__global__ void __launch_bounds__(256)
+coherent_batch_fp64_kernel(const BatchJob *jobs, int n_jobs,
+                           long long n_items, unsigned long long *counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long s_item;
+  __shared__ int s_job;
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const long long it = (long long)atomicAdd(counter, 1ull);
+      s_item = it;
+      s_job = it < n_items ? batch_find_job(jobs, n_jobs, it, true) : 0;
+    }
+    __syncthreads();
+    const long long it = s_item;
+    if (it >= n_items) break;
+    const BatchJob &J = jobs[s_job];
+    const long long local = it - J.item0;
+    coherent_fp64_cta(J.a, (int)(local % J.n_chunks),
+                      (int)(local / J.n_chunks), smem_raw);
+  }
+}
+
+int coherent_batch_fp64_launch(const BatchJob *jobs, int n_jobs,
+                               long long n_items, unsigned long long *counter,
+                               int threads, int ctas, size_t smem,
+                               cudaStream_t st) {
+  coherent_batch_fp64_kernel<<<ctas, threads, smem, st>>>(jobs, n_jobs,
+                                                           n_items, counter);
+  return cuda_status(cudaGetLastError(), "batch fp64 launch");
+}
+
+int batch_fp64_blocks_per_sm(int threads, size_t smem) {
+  static size_t limit = 0;
+  limit = std::max(limit, smem);
+  int n = 0;
+  if (cudaFuncSetAttribute(coherent_batch_fp64_kernel,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)limit) != cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &n, coherent_batch_fp64_kernel, threads, smem) != cudaSuccess)
+    return 0;
+  return n;
+}
+
 // ---------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------
@@ -245,14 +299,14 @@ extern "C" size_t ss_coherent_scratch_bytes(const ss_coherent_opts *opts,
   return ss::coherent_scratch(opts, n_traces, n_facets);
 }
 
-extern "C" int ss_coherent_fwd(const ss_coherent_opts *opts,
-                               const ss_facets *facets,
-                               const ss_traces *traces,
-                               const ss_pattern *pattern,
-                               const ss_roughness *rough,
-                               const ss_output *out, void *scratch,
-                               size_t scratch_bytes, void *stream) {
-  using namespace ss;
+namespace ss {
+
+// Validate one coherent call and fill its argument block (everything but
+// the scratch layout); shared by the one-call and the batched entry points.
+int build_co_args(const ss_coherent_opts *opts, const ss_facets *facets,
+                  const ss_traces *traces, const ss_pattern *pattern,
+                  const ss_roughness *rough, const ss_output *out, Plan &p,
+                  CoArgs &a) {
   if (!opts || !facets || !traces || !out) {
     set_error("null argument");
     return SS_ERR_ARG;
@@ -271,7 +325,6 @@ extern "C" int ss_coherent_fwd(const ss_coherent_opts *opts,
     set_error("unknown precision");
     return SS_ERR_ARG;
   }
-  Plan p;
   int s = coherent_plan(opts, T, N, &p);
   if (s) {
     set_error(s == SS_ERR_UNSUPPORTED ? "n_samples too large for the "
@@ -279,12 +332,7 @@ extern "C" int ss_coherent_fwd(const ss_coherent_opts *opts,
                                       : "bad sizes");
     return s;
   }
-  const size_t need = coherent_scratch(opts, T, N);
-  if (!scratch || scratch_bytes < need) {
-    set_error("scratch buffer too small");
-    return SS_ERR_SCRATCH;
-  }
-  CoArgs a{};
+  a = CoArgs{};
   a.F = *facets;
   a.pos = traces->pos;
   a.uct = traces->uct;
@@ -331,6 +379,31 @@ extern "C" int ss_coherent_fwd(const ss_coherent_opts *opts,
     a.sigma = rough->sigma;
     a.corr = rough->corr;
     a.fad = faddeeva_coeffs();
+  }
+  a.tb = p.tb;
+  a.n_chunks = p.n_chunks;
+  return SS_OK;
+}
+
+}  // namespace ss
+
+extern "C" int ss_coherent_fwd(const ss_coherent_opts *opts,
+                               const ss_facets *facets,
+                               const ss_traces *traces,
+                               const ss_pattern *pattern,
+                               const ss_roughness *rough,
+                               const ss_output *out, void *scratch,
+                               size_t scratch_bytes, void *stream) {
+  using namespace ss;
+  Plan p;
+  CoArgs a;
+  int s = build_co_args(opts, facets, traces, pattern, rough, out, p, a);
+  if (s) return s;
+  const int T = traces->n_traces, N = facets->n_facets;
+  const size_t need = coherent_scratch(opts, T, N);
+  if (!scratch || scratch_bytes < need) {
+    set_error("scratch buffer too small");
+    return SS_ERR_SCRATCH;
   }
   a.part = scratch;
   size_t hist = (size_t)p.n_chunks * T * a.n_seg *

@@ -15,6 +15,8 @@
 // Everything else (incidence, sincs, taper, antenna gain, roughness series)
 // runs in float32; histograms accumulate float32 per CTA chunk and chunks are
 // summed in float64 by the reduce kernel.
+#include <algorithm>
+
 #include "ss_coherent.cuh"
 #include "ss_df.cuh"
 #include "ss_f32.cuh"
@@ -37,18 +39,15 @@ __device__ __forceinline__ float dot_df(float xh, float xl, float yh, float yl,
   return s + lo;
 }
 
-struct SplitConsts {
-  float k, amp_pref, gamma, taper_inv;  // taper_inv = 1 / (2 s^2)
-  float K2h, K2l;                       // 2k as double-float
-  float Ah, Al, Bh, Bl;                 // u = r A - B, A = 2/(c dt), B = t0/dt
-  float fadL;
-  float sigma, corr;
-};
 
+// One CTA's work item: facet chunk `chunk` of trace block `group`. Shared
+// by the one-call kernel (item = block index) and the batched persistent
+// kernel (item pulled from a work queue).
 template <int ROUGH>
-__global__ void __launch_bounds__(256)
-coherent_split_kernel(CoArgs a, SplitConsts k) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
+                                                   const SplitConsts &k,
+                                                   int chunk, int group,
+                                                   unsigned char *smem_raw) {
   float2 *hist = reinterpret_cast<float2 *>(smem_raw);
   float *lg = reinterpret_cast<float *>(hist + (size_t)a.tb * a.n_seg);
   __shared__ float s_ph[SS_MAX_TB][3], s_pl[SS_MAX_TB][3];
@@ -61,8 +60,7 @@ coherent_split_kernel(CoArgs a, SplitConsts k) {
   __shared__ float s_fad[SS_FAD_N];
   __shared__ int s_rng[2];
 
-  const int chunk = blockIdx.x;
-  const int t_base = blockIdx.y * a.tb;
+  const int t_base = group * a.tb;
   const int nt = min(a.tb, a.T - t_base);
   const int tid = threadIdx.x;
   int pa_len = 0;
@@ -272,16 +270,104 @@ coherent_split_kernel(CoArgs a, SplitConsts k) {
     a.part_drop[(size_t)chunk * a.T + t_base + tid] = (double)s_drop[tid];
 }
 
-int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st) {
-  int pa_len = 0, pb_len = 0;
-  if (a.pat_kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
-  if (a.pat_kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
-  if (a.pat_kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * a.pat_n; pb_len = 4; }
-  if (a.pat_kind == SS_PAT_TABULATED) { pa_len = a.pat_n; pb_len = a.pat_n; }
-  if (pa_len + pb_len > SS_PAT_MAX) {
-    set_error("antenna table too large for the split kernel");
-    return SS_ERR_UNSUPPORTED;
+template <int ROUGH>
+__global__ void __launch_bounds__(256)
+coherent_split_kernel(CoArgs a, SplitConsts k) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  coherent_split_cta<ROUGH>(a, k, blockIdx.x, blockIdx.y, smem_raw);
+}
+
+// Batched persistent kernel: CTAs pull (job, trace block, facet chunk)
+// items from a global counter until the queue is empty, so jobs of very
+// different sizes share one launch without tail effects.
+template <int ROUGH>
+__global__ void __launch_bounds__(256)
+coherent_batch_split_kernel(const BatchJob *jobs, int n_jobs,
+                            long long n_items, unsigned long long *counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long s_item;
+  __shared__ int s_job;
+  for (;;) {
+    __syncthreads();  // the previous item's shared memory is free
+    if (threadIdx.x == 0) {
+      const long long it = (long long)atomicAdd(counter, 1ull);
+      s_item = it;
+      s_job = it < n_items ? batch_find_job(jobs, n_jobs, it, true) : 0;
+    }
+    __syncthreads();
+    const long long it = s_item;
+    if (it >= n_items) break;
+    const BatchJob &J = jobs[s_job];
+    const long long local = it - J.item0;
+    coherent_split_cta<ROUGH>(J.a, J.k, (int)(local % J.n_chunks),
+                              (int)(local / J.n_chunks), smem_raw);
   }
+}
+
+template <int ROUGH>
+static int batch_split_launch_r(const BatchJob *jobs, int n_jobs,
+                                long long n_items,
+                                unsigned long long *counter, int threads,
+                                int ctas, size_t smem, cudaStream_t st) {
+  // the dynamic shared-memory limit was raised at prepare time, so this
+  // path holds only stream operations (it may run under graph capture)
+  coherent_batch_split_kernel<ROUGH><<<ctas, threads, smem, st>>>(
+      jobs, n_jobs, n_items, counter);
+  return cuda_status(cudaGetLastError(), "batch split launch");
+}
+
+int coherent_batch_split_launch(const BatchJob *jobs, int n_jobs,
+                                long long n_items,
+                                unsigned long long *counter, int rough_kind,
+                                int threads, int ctas, size_t smem,
+                                cudaStream_t st) {
+  switch (rough_kind) {
+    case SS_ROUGH_NONE:
+      return batch_split_launch_r<SS_ROUGH_NONE>(jobs, n_jobs, n_items,
+                                                 counter, threads, ctas, smem,
+                                                 st);
+    case SS_ROUGH_GAUSS_FULL:
+      return batch_split_launch_r<SS_ROUGH_GAUSS_FULL>(
+          jobs, n_jobs, n_items, counter, threads, ctas, smem, st);
+    case SS_ROUGH_GAUSS_AREA:
+      return batch_split_launch_r<SS_ROUGH_GAUSS_AREA>(
+          jobs, n_jobs, n_items, counter, threads, ctas, smem, st);
+    default:
+      return batch_split_launch_r<SS_ROUGH_EXP_AREA>(
+          jobs, n_jobs, n_items, counter, threads, ctas, smem, st);
+  }
+}
+
+int batch_split_blocks_per_sm(int rough_kind, int threads, size_t smem) {
+  // raise the kernel's dynamic shared-memory limit to the largest size any
+  // prepared batch uses (never lowered: earlier batches stay launchable)
+  static size_t limit[4] = {0, 0, 0, 0};
+  const int r = rough_kind & 3;
+  limit[r] = std::max(limit[r], smem);
+  const int lim = (int)limit[r];
+  int n = 0;
+  cudaError_t e = cudaSuccess;
+  switch (rough_kind) {
+#define SS_OCC(R)                                                            \
+  case R:                                                                    \
+    e = cudaFuncSetAttribute(coherent_batch_split_kernel<R>,                 \
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,    \
+                             lim);                                           \
+    if (e == cudaSuccess)                                                    \
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(                     \
+          &n, coherent_batch_split_kernel<R>, threads, smem);                \
+    break;
+    SS_OCC(SS_ROUGH_NONE)
+    SS_OCC(SS_ROUGH_GAUSS_FULL)
+    SS_OCC(SS_ROUGH_GAUSS_AREA)
+    default:
+      SS_OCC(SS_ROUGH_EXP_AREA)
+#undef SS_OCC
+  }
+  return e == cudaSuccess ? n : 0;
+}
+
+SplitConsts coherent_split_consts(const CoArgs &a) {
   SplitConsts k{};
   k.k = (float)a.k;
   k.amp_pref = (float)(a.k / kTwoPi);
@@ -299,6 +385,20 @@ int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st) {
   k.fadL = (float)a.fad.L;
   k.sigma = (float)a.sigma;
   k.corr = (float)a.corr;
+  return k;
+}
+
+int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st) {
+  int pa_len = 0, pb_len = 0;
+  if (a.pat_kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
+  if (a.pat_kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
+  if (a.pat_kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * a.pat_n; pb_len = 4; }
+  if (a.pat_kind == SS_PAT_TABULATED) { pa_len = a.pat_n; pb_len = a.pat_n; }
+  if (pa_len + pb_len > SS_PAT_MAX) {
+    set_error("antenna table too large for the split kernel");
+    return SS_ERR_UNSUPPORTED;
+  }
+  const SplitConsts k = coherent_split_consts(a);
   dim3 grid(p.n_chunks, p.n_groups);
   size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2) +
                 (a.rough_kind ? (a.n_terms + 1) * sizeof(float) : 0);

@@ -1,5 +1,5 @@
 // Ordered reduction of per-CTA partial histograms into the output layout.
-#include "ss_internal.cuh"
+#include "ss_coherent.cuh"
 
 namespace ss {
 
@@ -36,6 +36,56 @@ __global__ void chunk_reduce_kernel(ReduceArgs r, ss_output out) {
       out.dropped[t] = d;
     }
   }
+}
+
+// Batched form: one grid-stride pass over every job's (trace, segment)
+// elements; each element sums its job's chunk partials in chunk order.
+template <typename P>
+__global__ void batch_reduce_kernel(const BatchJob *jobs, int n_jobs,
+                                    long long n_out) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+       e < n_out; e += (long long)gridDim.x * blockDim.x) {
+    const BatchJob &J = jobs[batch_find_job(jobs, n_jobs, e, false)];
+    const CoArgs &a = J.a;
+    const long long local = e - J.out0;
+    const int t = (int)(local / a.n_seg);
+    const int b = (int)(local % a.n_seg);
+    const P *part = reinterpret_cast<const P *>(a.part);
+    double sr = 0.0, si = 0.0;
+    for (int c = 0; c < J.n_chunks; ++c) {
+      const P v = part[((size_t)c * a.T + t) * a.n_seg + b];
+      sr += (double)v.x;
+      si += (double)v.y;
+    }
+    long o = (long)local;
+    if (a.split) {
+      const int side = b / a.n_samples, bl = b % a.n_samples;
+      o = ((long)t * a.n_samples + bl) * 2 + side;
+    }
+    if (J.out.field_c128) {
+      J.out.field_c128[2 * o] = sr;
+      J.out.field_c128[2 * o + 1] = si;
+    } else {
+      J.out.field_c64[2 * o] = (float)sr;
+      J.out.field_c64[2 * o + 1] = (float)si;
+    }
+    if (b == 0) {
+      double d = 0.0;
+      for (int c = 0; c < J.n_chunks; ++c)
+        d += a.part_drop[(size_t)c * a.T + t];
+      J.out.dropped[t] = d;
+    }
+  }
+}
+
+int batch_reduce_launch(const BatchJob *jobs, int n_jobs, long long n_out,
+                        bool f64_parts, cudaStream_t st) {
+  const int grid = 4 * sm_count();
+  if (f64_parts)
+    batch_reduce_kernel<double2><<<grid, 256, 0, st>>>(jobs, n_jobs, n_out);
+  else
+    batch_reduce_kernel<float2><<<grid, 256, 0, st>>>(jobs, n_jobs, n_out);
+  return cuda_status(cudaGetLastError(), "batch reduce launch");
 }
 
 int sm_count() {

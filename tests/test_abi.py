@@ -44,7 +44,13 @@ def test_struct_layouts_match_header(tmp_path):
                "ss_pattern": _lib.Pattern, "ss_roughness": _lib.Roughness,
                "ss_coherent_opts": _lib.CoherentOpts,
                "ss_output": _lib.Output, "ss_interface": _lib.Interface,
-               "ss_refracted_opts": _lib.RefractedOpts}
+               "ss_refracted_opts": _lib.RefractedOpts,
+               "ss_waveform_opts": _lib.WaveformOpts,
+               "ss_multifreq_opts": _lib.MultifreqOpts,
+               "ss_adjoint_io": _lib.AdjointIO,
+               "ss_coherent_job": _lib.CoherentJob,
+               "ss_batch_tuning": _lib.BatchTuning,
+               "ss_batch_info": _lib.BatchInfo}
     lines = ["#include <stdio.h>", "#include <stddef.h>",
              '#include "soundersim_gb300.h"', "int main(void) {"]
     for cname, py in structs.items():

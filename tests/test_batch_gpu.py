@@ -1,0 +1,96 @@
+"""Batched persistent launch of many coherent jobs (work queue + batched
+reduce), its CUDA-graph replay and the autotuner, against the float64
+oracle per job and against the one-call entry point."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import lpa
+from radar_sounder_simulator_gb300.batch import CoherentBatch
+from radar_sounder_simulator_gb300.coherent import prepare_coherent
+from tests.util import facets_from, field_errors
+
+pytestmark = pytest.mark.gpu
+C = 299792458.0
+
+
+@pytest.fixture(scope="module")
+def jobs(golden):
+    g = golden("coherent")
+    f = facets_from(g, "surf")
+    base = dict(k=float(g["k"]), gamma=-0.279, t0=float(g["t0"]),
+                dt=float(g["dt"]), n_samples=int(g["n_samples"]), c=C)
+    full = (g["pos"], g["uct"], f.centers, f.normals, f.areas, f.e1, f.e2)
+    few = (g["pos"][:5], g["uct"][:5], f.centers, f.normals, f.areas, f.e1,
+           f.e2)
+    pat = ("array", g["ant_pv"], g["ant_pa"], g["ant_pb"])
+    return [
+        (full, dict(base)),
+        (few, dict(base, k=1.7 * float(g["k"]), block_size=96)),
+        (full, dict(base, split_sides=True, taper_s=0.05)),
+        (full, dict(base, pattern=pat)),
+        (full, dict(base, gamma=g["gamma_facet"])),
+        (full, dict(base, interp_bins=True, n_samples=int(g["n_samples"]) // 2)),
+    ]
+
+
+def _run(jobs, precision, tuning=None):
+    plans = [prepare_coherent(*a, **kw, precision=precision)
+             for a, kw in jobs]
+    b = CoherentBatch(plans, tuning)
+    b.run()
+    return b, b.to_numpy(np.complex128)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_batch_matches_oracle_and_one_call(jobs, precision):
+    b, res = _run(jobs, precision)
+    assert b.info.n_jobs == len(jobs) and b.info.n_items >= len(jobs)
+    for (args, kw), (got, drop) in zip(jobs, res):
+        ref, ref_drop = lpa.coherent_cluttergram(*args, **kw)
+        assert got.shape == ref.shape
+        scale = np.abs(ref).max()
+        if precision == "fp64":
+            assert np.abs(got - ref).max() <= 1e-9 * scale
+        else:
+            e = field_errors(got, ref)
+            assert e["rel_l2"] <= 1e-4 and e["phase_rad"] <= 1e-3 and \
+                e["power_db"] <= 0.01, e
+        one = prepare_coherent(*args, **kw, precision=precision)
+        f1, d1 = one.to_numpy(*one.run(), np.complex128)
+        tol = 1e-12 if precision == "fp64" else 2e-6
+        assert np.abs(got - f1).max() <= tol * scale
+        np.testing.assert_allclose(drop, d1, rtol=1e-5, atol=1e-9 * scale ** 2)
+
+
+def test_graph_replay_and_tunings_agree(jobs):
+    b, res = _run(jobs, "split", tuning=(128, 2, 64, 0))
+    ref = [f.clone() for f, _ in b.outputs]
+    for f, d in b.outputs:
+        f.zero_()
+        d.zero_()
+    b.capture()
+    for f, d in b.outputs:
+        f.zero_()
+    b.replay()
+    torch.cuda.synchronize()
+    for (f, _), r in zip(b.outputs, ref):
+        assert torch.allclose(f, r, rtol=0, atol=2e-6 * r.abs().max().item())
+    tun, ms = b.autotune(candidates=[(256, 8, 16, 0), (128, 4, 4, 0),
+                                     (256, 2, 64, 1)], reps=1)
+    assert ms > 0 and tun in [(256, 8, 16, 0), (128, 4, 4, 0), (256, 2, 64, 1)]
+    b.run()
+    torch.cuda.synchronize()
+    for (f, _), r in zip(b.outputs, ref):
+        assert torch.allclose(f, r, rtol=0, atol=2e-6 * r.abs().max().item())
+
+
+def test_batch_rejects_mixed_roughness(jobs, golden):
+    g = golden("coherent")
+    args, kw = jobs[0]
+    plans = [prepare_coherent(*args, **kw, precision="split"),
+             prepare_coherent(*args, **kw, precision="split",
+                              roughness=(0.3, 4.0, g["phasors"], 40))]
+    with pytest.raises(ValueError):
+        CoherentBatch(plans)
