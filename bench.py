@@ -48,6 +48,10 @@ def parse():
                     help="DRAM bytes per launch of the dominant kernel from "
                          "an ncu capture of the same workload (reported in "
                          "the roofline object)")
+    ap.add_argument("--rows", default="cfg1,modef,cfg3,cfg4,cfg5",
+                    help="secondary workloads measured after the headline "
+                         "(comma list, or 'none')")
+    ap.add_argument("--batch-instances", type=int, default=96)
     ap.add_argument("--fp64-traces", type=int, default=256,
                     help="traces of the float64-form step (its rate is per "
                          "pair; the error check covers these traces)")
@@ -389,6 +393,7 @@ def main():
                                         os.cpu_count() or 1)
             cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1,
                    "kind": "port", "sample": sample}
+        rows = run_rows(args, device) if ws == 1 else None
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": ms, "higher_is_better": True,
@@ -405,10 +410,290 @@ def main():
                 "per_kernel_ms": dict(zip(["surface", "h1_seq", "h2_joint",
                                            "bed_joint"], per_kernel)),
                 "gpu_launches": launches, "roofline": roof,
-                "clocks": clk.summary(), "cpu_baseline": cpu}
+                "clocks": clk.summary(), "cpu_baseline": cpu, "rows": rows}
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+# --------------------------------------------------------------------------
+# secondary workloads (the other configurations), measured after the line's
+# headline on rank 0; each entry states its own units and errors
+# --------------------------------------------------------------------------
+def _events_ms(fn, reps, flush=None):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        if flush is not None:
+            flush.fill_(1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return float(np.median(ts))
+
+
+def _complex(field):
+    import torch
+    return torch.view_as_complex(field.contiguous())
+
+
+def _errors(a, b):
+    """rel L2, max phase and max dB over samples above -60 dB of the peak."""
+    import torch
+    rel = (torch.linalg.vector_norm(a - b) /
+           torch.linalg.vector_norm(b)).item()
+    p = b.abs() ** 2
+    keep = p > p.max() * 1e-6
+    ph = torch.angle(a[keep] / b[keep]).abs().max().item()
+    db = (10 * torch.log10(a[keep].abs() ** 2 / p[keep])).abs().max().item()
+    return {"rel_l2": rel, "phase_rad": ph, "power_db": db}
+
+
+def row_cfg1(device, flush):
+    """Plain surface, delta-binned coherent sum + LFM pulse compression."""
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.coherent import prepare_coherent
+    from radar_sounder_simulator_gb300.waveform import (compress_tensor,
+                                                         compressed_pulse)
+    cfg = scenes.config1()
+    f = cfg.facets
+    args = (cfg.pos, cfg.uct, f.centers, f.normals, f.areas, f.e1, f.e2)
+    pl = {p: prepare_coherent(*args, **cfg.kw, precision=p, device=device)
+          for p in ("split", "fp64")}
+    pulse, m = compressed_pulse(cfg.bw, cfg.pulse_length, cfg.kw["dt"],
+                                "hann", "chirp")
+    out = {}
+
+    def step(prec):
+        fld, _ = pl[prec].run()
+        out[prec] = compress_tensor(fld, pulse, m)
+    ms = _events_ms(lambda: step("split"), 5, flush)
+    ms64 = _events_ms(lambda: step("fp64"), 2, flush)
+    fld, _ = pl["split"].run()
+    ms_rc = _events_ms(lambda: compress_tensor(fld, pulse, m), 5, flush)
+    pairs = len(f.centers) * len(cfg.pos)
+    T, B = len(cfg.pos), cfg.kw["n_samples"]
+    return {"workload": "surface_128sq_100m_256tr_2048bins_chirp_20us",
+            "unit": "contribs/s", "value": pairs / (ms * 1e-3),
+            "ms_per_step": ms, "fp64_value": pairs / (ms64 * 1e-3),
+            "split_over_fp64": ms64 / ms,
+            "range_compression": {"taps": len(pulse), "ms": ms_rc,
+                                  "samples_per_s": T * B / (ms_rc * 1e-3)},
+            "error_vs_fp64": _errors(out["split"], out["fp64"])}
+
+
+def row_modef(device, flush):
+    """Frequency-sampled synthesis of the config-1 scene, K = 1024."""
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.multifreq import prepare_multifreq
+    cfg = scenes.config1()
+    f = cfg.facets
+    tw = cfg.kw["t0"] + np.arange(cfg.kw["n_samples"]) * cfg.kw["dt"]
+    res, ms = {}, {}
+    for prec in ("split", "fp64"):
+        pl = prepare_multifreq(cfg.pos, f.centers, f.normals, f.areas, f.e1,
+                               f.e2, gamma=cfg.kw["gamma"], f0=cfg.f0,
+                               bandwidth=cfg.bw, c=cfg.kw["c"], twtt=tw,
+                               n_freq=1024, freeze_amplitudes=True,
+                               precision=prec, device=device)
+        ms[prec] = _events_ms(pl.run, 3 if prec == "split" else 1, flush)
+        res[prec] = _complex(pl.run())
+    units = len(f.centers) * len(cfg.pos) * 1024
+    return {"workload": "surface_128sq_100m_256tr_K1024_frozen",
+            "unit": "pair-frequencies/s", "value": units / (ms["split"] * 1e-3),
+            "ms_per_step": ms["split"],
+            "fp64_value": units / (ms["fp64"] * 1e-3),
+            "split_over_fp64": ms["fp64"] / ms["split"],
+            "error_vs_fp64": _errors(res["split"], res["fp64"])}
+
+
+def row_cfg3(device, flush):
+    """Rough surface and bed, four bands: per band the surface coherent sum
+    and the refracted bed sum (per-facet sigma, l; exponential ACF with the
+    area-only series and taper), each pulse-compressed."""
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.coherent import prepare_coherent
+    from radar_sounder_simulator_gb300.multilayer import prepare_refracted
+    from radar_sounder_simulator_gb300.waveform import (compress_tensor,
+                                                         compressed_pulse)
+    cfg = scenes.config3()
+    s, b = cfg.surface, cfg.bed
+    c = cfg.c
+    bands = {}
+    total_ms, total_pairs = 0.0, 0
+    for f0 in cfg.bands:
+        bw = cfg.frac_bw * f0
+        dt = 1.0 / (2.0 * bw)
+        k0 = 2 * np.pi * f0 / c
+        n_s = int(np.ceil(2 * (1000.0 * np.sqrt(3.15) + 3000.0) / c / dt))
+        t0 = scenes.window(cfg.pos, s.centers, n_samples=n_s, dt=dt)
+        rs, rb = cfg.rough["surface"], cfg.rough["bed"]
+        nt_s = scenes.n_terms_for((2 * k0 * rs["sigma"].max()) ** 2)
+        nt_b = scenes.n_terms_for((2 * k0 * np.sqrt(3.15) *
+                                   np.quantile(rb["sigma"], 0.999)) ** 2)
+        ps = prepare_coherent(
+            cfg.pos, cfg.uct, s.centers, s.normals, s.areas, s.e1, s.e2,
+            k=k0, gamma=cfg.gamma_surface, t0=t0, dt=dt, n_samples=n_s, c=c,
+            roughness=(rs["sigma"], rs["corr"], rs["phasors"], nt_s,
+                       "exponential"), d_phi_area=True, taper_s=0.05,
+            precision="split", device=device)
+        pb = prepare_refracted(
+            cfg.pos, cfg.uct, b, [s], cfg.eps, cfg.att, mode="coherent",
+            t0=t0, dt=dt, n_samples=n_s, c=c, gamma=cfg.gamma_bed, k0=k0,
+            roughness=(rb["sigma"], rb["corr"], rb["phasors"], nt_b,
+                       "exponential"), d_phi_area=True, taper_s=0.05,
+            refraction="sequential", precision="split", device=device)
+        pulse, m = compressed_pulse(bw, 10e-6, dt, "hann", "chirp")
+
+        def step():
+            f1, _ = ps.run()
+            f2, _ = pb.run()
+            compress_tensor(f1, pulse, m)
+            compress_tensor(f2, pulse, m)
+        ms = _events_ms(step, 2, flush)
+        pairs = (len(s.centers) + len(b.centers)) * len(cfg.pos)
+        bands[f"{f0 / 1e6:.0f}MHz"] = {"ms": ms, "n_terms": [nt_s, nt_b],
+                                       "n_samples": n_s,
+                                       "contribs_per_s": pairs / (ms * 1e-3)}
+        total_ms += ms
+        total_pairs += pairs
+        del ps, pb
+    return {"workload": "rough_surface_bed_512sq_25m_2048tr_4bands",
+            "unit": "contribs/s", "value": total_pairs / (total_ms * 1e-3),
+            "ms_per_step": total_ms, "bands": bands}
+
+
+def row_cfg4(device, n_inst, flush):
+    """Batched design sweep: one persistent work-queue launch over all
+    instances, captured in a CUDA graph, autotuned decomposition."""
+    import torch
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.batch import CoherentBatch
+    from radar_sounder_simulator_gb300.coherent import prepare_coherent
+    t_host = time.perf_counter()
+    plans, plans64, pairs = [], [], 0
+    for i in range(n_inst):
+        inst = scenes.config4_instance(i)
+        f = inst.facets
+        args = (inst.pos, inst.uct, f.centers, f.normals, f.areas, f.e1,
+                f.e2)
+        p = prepare_coherent(*args, **inst.kw, precision="split",
+                             device=device)
+        plans.append(p)
+        pairs += int(np.sum(np.minimum(
+            (p.cull.off.astype(np.int64) + p.cull.n_win) * p.cull.block_size,
+            p.N) - np.minimum(p.cull.off.astype(np.int64) *
+                              p.cull.block_size, p.N)))
+        if i < 8:
+            plans64.append(prepare_coherent(*args, **inst.kw,
+                                            precision="fp64", device=device))
+    host_s = time.perf_counter() - t_host
+    batch = CoherentBatch(plans)
+    tun, tune_ms = batch.autotune(
+        candidates=[(256, 8, 16, 0), (256, 4, 16, 0), (128, 8, 16, 0),
+                    (256, 8, 4, 0), (256, 8, 64, 0), (128, 4, 64, 0)],
+        reps=1)
+    batch.capture()
+    ms = _events_ms(batch.replay, 3, flush)
+    # FP64 form and error on the first 8 instances (one-call entry point
+    # against the batch's split output)
+    sub_pairs = sum(p.T * min(p.cull.n_win * p.cull.block_size, p.N)
+                    for p in plans64)
+    b64 = CoherentBatch(plans64)
+    ms64 = _events_ms(b64.run, 1, flush)
+    bsp = CoherentBatch(plans[:8])
+    bsp.run()
+    b64.run()
+    torch.cuda.synchronize()
+    err = {"rel_l2": 0.0, "phase_rad": 0.0, "power_db": 0.0}
+    for (fs, _), (fd, _) in zip(bsp.outputs, b64.outputs):
+        e = _errors(_complex(fs), _complex(fd))
+        err = {k: max(err[k], e[k]) for k in err}
+    ms_sub = _events_ms(bsp.run, 2, flush)
+    return {"workload": f"design_sweep_{n_inst}_instances",
+            "unit": "contribs/s", "value": pairs / (ms * 1e-3),
+            "ms_per_step": ms, "pairs": pairs, "launches_per_step": 2,
+            "cuda_graph": True, "tuning": list(tun),
+            "host_prep_s": host_s,
+            "fp64_subset": {"instances": len(plans64),
+                            "split_ms": ms_sub, "fp64_ms": ms64,
+                            "split_over_fp64": ms64 / ms_sub,
+                            "window_pairs": sub_pairs},
+            "error_vs_fp64": err}
+
+
+def row_cfg5(device, flush):
+    """Adjoint: forward bed power and hand-written backward of the dB
+    misfit, 512^2 bed facets x 1024 traces."""
+    import torch
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.adjoint import (WindowPowerModel,
+                                                       db_misfit)
+    cfg = scenes.config5()
+    model = WindowPowerModel(
+        cfg.pos, cfg.uct, cfg.bed, [cfg.surface], cfg.eps, [0.0, cfg.alpha],
+        t0=cfg.t0, dt=cfg.dt, n_samples=cfg.n_samples, c=cfg.c, k0=cfg.k0,
+        window=cfg.window, alpha_legs=(1,), corr_length=cfg.corr,
+        phasors=cfg.phasors, n_terms=cfg.n_terms, precision="split",
+        device=device)
+    dev = model.device
+    with torch.no_grad():
+        P_hat = model.power(torch.tensor(cfg.R_hat, device=dev),
+                            torch.tensor(cfg.sig_hat, device=dev),
+                            torch.tensor(cfg.alpha + 1.0, device=dev))
+    R = torch.tensor(cfg.R, device=dev, requires_grad=True)
+    sg = torch.tensor(cfg.sig, device=dev, requires_grad=True)
+    a = torch.tensor(cfg.alpha, dtype=torch.float64, device=dev,
+                     requires_grad=True)
+    ts = {}
+
+    def fwd():
+        return db_misfit(model.power(R, sg, a), P_hat)
+    ts["forward_ms"] = _events_ms(fwd, 2, flush)
+    L = fwd()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    L.backward()
+    e1.record()
+    torch.cuda.synchronize()
+    ts["backward_ms"] = e0.elapsed_time(e1)
+    pairs = len(cfg.bed.centers) * len(cfg.pos)
+    return {"workload": "adjoint_bed_512sq_1024tr", "unit": "contribs/s",
+            "value": pairs / (ts["backward_ms"] * 1e-3), **ts,
+            "n_terms": cfg.n_terms,
+            "grad_norms": {"reflectivity_db": float(R.grad.norm()),
+                           "rms_height": float(sg.grad.norm()),
+                           "alpha": float(a.grad)}}
+
+
+def run_rows(args, device):
+    import torch
+    want = [] if args.rows == "none" else args.rows.split(",")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
+    rows = {}
+    fns = {"cfg1": lambda: row_cfg1(device, flush),
+           "modef": lambda: row_modef(device, flush),
+           "cfg3": lambda: row_cfg3(device, flush),
+           "cfg4": lambda: row_cfg4(device, args.batch_instances, flush),
+           "cfg5": lambda: row_cfg5(device, flush)}
+    for name in want:
+        t0 = time.perf_counter()
+        try:
+            rows[name] = fns[name]()
+        except Exception as exc:  # reported, not hidden: the line still prints
+            rows[name] = {"error": f"{type(exc).__name__}: {exc}"}
+        rows[name]["wall_s"] = time.perf_counter() - t0
+        torch.cuda.empty_cache()
+    return rows
+
 
 
 def split_error(outs, outs64):

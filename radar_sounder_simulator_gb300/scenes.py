@@ -98,7 +98,9 @@ def firn_n_eff(depth, rho_surface=350.0, rho_ice=917.0, scale=30.0):
 
 def window(pos, centers, *, n_samples, dt, lead_m=200.0, c=C_LIGHT):
     """t0 = 2 (min slant range - lead) / c (the configs' window rule)."""
-    r = np.linalg.norm(pos[:, None, :] - centers[None, ::97], axis=-1).min()
+    step = max(1, len(pos) // 256)
+    r = np.linalg.norm(pos[::step, None, :] - centers[None, ::97],
+                       axis=-1).min()
     return 2.0 * (r - lead_m) / c
 
 
@@ -157,6 +159,117 @@ def config2(seed=2, n_cells=512, n_traces=1024, spacing=50.0,
         pos=pos, uct=uct, eps=eps, att=att, gammas=gammas, f0=f0, bw=bw,
         k0=2 * np.pi * f0 / C_LIGHT, t0=t0, dt=dt, n_samples=2048,
         c=C_LIGHT, refraction="joint")
+
+
+def n_terms_for(x_max):
+    """D_Phi series length for the largest (sigma K)^2 of a run:
+    ceil(x + 6 sqrt(x) + 5) clipped to [10, 300] (roughness.py:189-196)."""
+    x = float(x_max)
+    return int(np.clip(np.ceil(x + 6.0 * np.sqrt(x) + 5.0), 10, 300))
+
+
+def speckle_phasors(n, rng):
+    """Unit-variance complex Gaussian speckle phasors (roughness.py:199-204
+    form), complex64."""
+    ph = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    return (ph / np.sqrt(2.0)).astype(np.complex64)
+
+
+def config3(seed=3, n_cells=512, n_traces=2048, spacing=25.0,
+            bed_depth=1000.0):
+    """Sub-facet roughness, multi-frequency: the config-1 statistics
+    (exponential ACF 1 km, 50 m rms) over the same 12.8 km square at 25 m
+    facets (512^2, inside the 450 MHz LPA facet limit at 20 km), surface and
+    a bed under ``bed_depth`` m of ice; per-facet bed rms height log-normal
+    (median 0.3 m, sigma_log 0.7), correlation length U[5, 50] m,
+    exponential ACF (area-only D_Phi with the 0.05 taper); surface rms
+    U[0.05, 0.5] m with the same correlation lengths; 2048 traces at 20 km;
+    bands at 30, 60, 150 and 450 MHz of 10% bandwidth."""
+    rng = np.random.default_rng(seed)
+    surf = surface(n_cells, spacing, 50.0, 1000.0, 0.0, rng)
+    bed = surface(n_cells, spacing, 50.0, 1000.0, -bed_depth, rng)
+    n = n_cells * n_cells
+    pos, uct = straight_track(n_traces, 12800.0 / n_traces, 20000.0)
+    eps = [1.0, 3.15]
+    rough = dict(
+        surface=dict(sigma=rng.uniform(0.05, 0.5, n),
+                     corr=rng.uniform(5.0, 50.0, n),
+                     phasors=speckle_phasors(n, rng)),
+        bed=dict(sigma=np.exp(np.log(0.3) + 0.7 * rng.standard_normal(n)),
+                 corr=rng.uniform(5.0, 50.0, n),
+                 phasors=speckle_phasors(n, rng)))
+    bands = [30e6, 60e6, 150e6, 450e6]
+    return SimpleNamespace(surface=surf, bed=bed, pos=pos, uct=uct, eps=eps,
+                           att=[0.0, 10.0], rough=rough, bands=bands,
+                           frac_bw=0.10, n_freq=1024, c=C_LIGHT,
+                           gamma_surface=fresnel_normal(1.0, 3.15),
+                           gamma_bed=fresnel_normal(3.15, 9.0))
+
+
+def gaussian_beam_table(beamwidth_deg, n=64):
+    """Tabulated one-way field gain of a Gaussian beam whose two-way power
+    is -3 dB at half the beamwidth: g(theta) = 2^(-(theta/theta_h)^2 / 4)
+    (g^4 = 1/2 at theta_h). Returns (angles (n,), gains (n,)) over
+    [0, pi/2], the ``tabulated`` pattern's (pa, pb)."""
+    th = np.linspace(0.0, np.pi / 2, n)
+    th_h = np.radians(beamwidth_deg) / 2.0
+    return th, 2.0 ** (-((th / th_h) ** 2) / 4.0)
+
+
+def config4_instance(i, n_samples=2048, facet_m=25.0):
+    """One instance of the batched design sweep (seed 4000 + i): altitude
+    U[12, 25] km, centre frequency log-uniform in [30, 450] MHz with 15%
+    bandwidth, beamwidth U[20, 90] deg (Gaussian tabulated pattern, boresight
+    nadir), U{256..4096} traces at 25 m, U{256..1024}^2 facets of 25 m with
+    the config-1 statistics (exponential ACF 1 km, 50 m rms)."""
+    rng = np.random.default_rng(4000 + i)
+    alt = rng.uniform(12e3, 25e3)
+    f0 = float(np.exp(rng.uniform(np.log(30e6), np.log(450e6))))
+    bw = 0.15 * f0
+    beam = rng.uniform(20.0, 90.0)
+    T = int(rng.integers(256, 4097))
+    ncell = int(rng.integers(256, 1025))
+    f = surface(ncell, facet_m, 50.0, 1000.0, 0.0, rng)
+    pos, uct = straight_track(T, 25.0, alt)
+    dt = 1.0 / (2.0 * bw)
+    t0 = window(pos, f.centers, n_samples=n_samples, dt=dt)
+    pa, pb = gaussian_beam_table(beam)
+    pv = np.tile([0.0, 0.0, -1.0], (T, 1))
+    kw = dict(k=2 * np.pi * f0 / C_LIGHT, gamma=fresnel_normal(1.0, 3.15),
+              t0=t0, dt=dt, n_samples=n_samples, c=C_LIGHT,
+              pattern=("tabulated", pv, pa, pb))
+    return SimpleNamespace(facets=f, pos=pos, uct=uct, kw=kw, f0=f0,
+                           beam=beam, T=T, n_cells=ncell)
+
+
+def config5(seed=5, n_cells=512, n_traces=1024, spacing=25.0,
+            bed_depth=1000.0):
+    """Differentiation: the config-3 scene geometry (surface over a bed under
+    ``bed_depth`` m of ice, 512^2 facets of 25 m each), 1024 traces at
+    20 km, 60 MHz; bed reflectivity R ~ U[-30, -5] dB, rms height
+    log-normal (median 0.3 m, sigma_log 0.7), correlation length 10 m,
+    attenuation 10 dB/km; the target radargram comes from R + N(0, 1 dB),
+    sigma x exp(N(0, 0.1)) and alpha + 1 dB/km."""
+    rng = np.random.default_rng(seed)
+    surf = surface(n_cells, spacing, 50.0, 1000.0, 0.0, rng)
+    bed = surface(n_cells, spacing, 50.0, 1000.0, -bed_depth, rng)
+    n = n_cells * n_cells
+    pos, uct = straight_track(n_traces, 12800.0 / n_traces, 20000.0)
+    f0 = 60e6
+    dt = 1.0 / (2.0 * 15e6)
+    t0 = 2.0 * (20000.0 - 200.0) / C_LIGHT
+    R = rng.uniform(-30.0, -5.0, n)
+    sig = np.exp(np.log(0.3) + 0.7 * rng.standard_normal(n))
+    R_hat = R + rng.standard_normal(n)
+    sig_hat = sig * np.exp(0.1 * rng.standard_normal(n))
+    k_ice = 2 * np.pi * f0 / C_LIGHT * np.sqrt(3.15)
+    n_terms = n_terms_for((2.0 * k_ice * np.quantile(sig, 0.999)) ** 2)
+    return SimpleNamespace(surface=surf, bed=bed, pos=pos, uct=uct,
+                           eps=[1.0, 3.15], alpha=10.0, k0=2 * np.pi * f0 /
+                           C_LIGHT, t0=t0, dt=dt, n_samples=1024, c=C_LIGHT,
+                           R=R, sig=sig, R_hat=R_hat, sig_hat=sig_hat, window=(0, 1024),
+                           corr=10.0, phasors=speckle_phasors(n, rng),
+                           n_terms=n_terms)
 
 
 def smoke_scene():
