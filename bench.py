@@ -44,10 +44,11 @@ def parse():
                     help="skip the float64-form step and the error check")
     ap.add_argument("--skip-e2e", action="store_true",
                     help="skip the drop-in (host buffers) step")
-    ap.add_argument("--traffic", type=float, default=None,
+    ap.add_argument("--traffic", type=float, default=184.5e6,
                     help="DRAM bytes per launch of the dominant kernel from "
                          "an ncu capture of the same workload (reported in "
-                         "the roofline object)")
+                         "the roofline object; default: the one-pass capture "
+                         "of the bed launch at the default size)")
     ap.add_argument("--rows", default="cfg1,modef,cfg3,cfg4,cfg5",
                     help="secondary workloads measured after the headline "
                          "(comma list, or 'none')")
