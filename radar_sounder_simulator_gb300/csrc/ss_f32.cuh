@@ -154,6 +154,24 @@ __device__ __forceinline__ float f_factor32(const float *fa, float L, float m,
   return 1.0f - ey2 * cr + 1.77245385091f * (t1 - t2);
 }
 
+// Terms of the D_Phi series that can matter in float32. The Poisson weight
+// x^m e^-x / m! of term m peaks at m ~ x with width sqrt(x); more than
+// 12 sqrt(x) + 12 below the peak it is under e^-72 of the peak term, and
+// every W_m grows at most algebraically towards small m, so the low terms
+// are skipped for all kinds. Above the peak only the exponential-ACF
+// weight W_m = 2 pi l^2 m (m^2 + (k_B l)^2)^(-3/2) Lx Ly is known to stay
+// algebraic (the Gaussian weights carry exp(-c/m), which grows with m), so
+// the high terms are skipped for that kind only; the reference's fixed
+// length n_terms caps the range.
+template <int KIND>
+__device__ __forceinline__ void d_phi_range(float x, int n_terms, int &m_lo,
+                                            int &m_hi) {
+  const float half = 12.0f * sqrtf(x) + 12.0f;
+  m_lo = max(1, (int)floorf(x - half));
+  m_hi = KIND == SS_ROUGH_EXP_AREA ? min(n_terms, (int)ceilf(x + half))
+                                   : n_terms;
+}
+
 // D_Phi in float32; lg[m] = lgamma(m + 1).
 template <int KIND>
 __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
@@ -166,11 +184,13 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
   if (!(x > 0.0f)) return 0.0f;
   const float logx = __logf(x);
   const float kb2 = A0 * A0 + B0 * B0;
+  int m_lo, m_hi;
+  d_phi_range<KIND>(x, n_terms, m_lo, m_hi);
   float acc = 0.0f;
   if (KIND == SS_ROUGH_GAUSS_AREA) {
     const float c = 0.25f * kb2 * l * l;
     const float pref = 3.14159265359f * l * l * Lx * Ly;
-    for (int m = 1; m <= n_terms; ++m) {
+    for (int m = m_lo; m <= m_hi; ++m) {
       const float mf = (float)m;
       const float im = __fdividef(1.0f, mf);
       const float e = __fmaf_rn(mf, logx, -lg[m]) - x - c * im;
@@ -179,7 +199,7 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
   } else if (KIND == SS_ROUGH_EXP_AREA) {
     const float pref = 6.28318530718f * l * l * Lx * Ly;
     const float kl2 = kb2 * l * l;
-    for (int m = 1; m <= n_terms; ++m) {
+    for (int m = m_lo; m <= m_hi; ++m) {
       const float mf = (float)m;
       const float im = __fdividef(1.0f, mf);
       const float im2 = im * im;
@@ -189,7 +209,7 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
     }
   } else {
     const float l4 = (l * l) * (l * l);
-    for (int m = 1; m <= n_terms; ++m) {
+    for (int m = m_lo; m <= m_hi; ++m) {
       const float mf = (float)m;
       const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
       const float w = __expf(e);
@@ -216,8 +236,10 @@ __device__ __forceinline__ float d_phi32_dx(int n_terms, const float *lg,
   if (!(x > 0.0f)) return 0.0f;
   const float logx = __logf(x);
   const float kb2 = A0 * A0 + B0 * B0;
+  int m_lo, m_hi;
+  d_phi_range<KIND>(x, n_terms, m_lo, m_hi);
   float acc = 0.0f, accm = 0.0f;
-  for (int m = 1; m <= n_terms; ++m) {
+  for (int m = m_lo; m <= m_hi; ++m) {
     const float mf = (float)m;
     const float im = __fdividef(1.0f, mf);
     const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
