@@ -66,6 +66,29 @@ def dist_env():
     return ws, rank, local
 
 
+def line_offset(rank):
+    """Cross-track offset of rank ``rank``'s flight line (m): each GPU flies
+    its own line over the shared scene, so ranks share no work and no
+    exchange (weak scaling, no collective on the data path)."""
+    return 200.0 * rank
+
+
+def max_over_ranks(ms, device, ws):
+    """The slowest rank's step time (the job's time); identity at ws = 1."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    if ws > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(pairs_per_rank, ws, ms_max):
+    """Whole-job contributions/s: every rank's pairs over the slowest
+    rank's time."""
+    return pairs_per_rank * ws / (ms_max * 1e-3)
+
+
 def config_dict(args, ws):
     return {"workload": WORKLOAD, "layers": 4,
             "facets_per_layer": args.n_cells ** 2, "facet_m": 50.0,
@@ -296,7 +319,7 @@ def main():
 
     from radar_sounder_simulator_gb300 import scenes
     cfg = scenes.config2(n_cells=args.n_cells, n_traces=args.n_traces,
-                         line_offset_y=200.0 * rank)
+                         line_offset_y=line_offset(rank))
     pairs_step = sum(len(f.centers) for f in cfg.layers) * len(cfg.pos)
 
     plans = build_plans(cfg, "split", device)
@@ -334,11 +357,8 @@ def main():
     if ws > 1:
         dist.barrier()
     ms = t_start.elapsed_time(t_end) / args.steps
-    ms_t = torch.tensor([ms], device=device, dtype=torch.float64)
-    if ws > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    value = pairs_step * ws / (ms * 1e-3)
+    ms = max_over_ranks(ms, device, ws)
+    value = job_rate(pairs_step, ws, ms)
     per_kernel = [float(np.mean([ev[s][i][0].elapsed_time(ev[s][i][1])
                                  for s in range(args.steps)]))
                   for i in range(len(plans))]
@@ -349,7 +369,7 @@ def main():
     err = None
     if not args.skip_fp64:
         sub = scenes.config2(n_cells=args.n_cells, n_traces=args.n_traces,
-                             line_offset_y=200.0 * rank)
+                             line_offset_y=line_offset(rank))
         nt = min(args.fp64_traces, args.n_traces)
         sub.pos, sub.uct = cfg.pos[:nt], cfg.uct[:nt]
         sub.t0 = cfg.t0
