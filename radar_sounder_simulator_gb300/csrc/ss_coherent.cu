@@ -236,7 +236,11 @@ int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p) {
     return SS_ERR_ARG;
   const int n_seg = o->n_samples * (o->split_sides ? 2 : 1);
   const size_t elt = o->precision == SS_PREC_FP64 ? 16 : 8;
-  const size_t budget = o->precision == SS_PREC_FP64 ? 96 * 1024 : 100 * 1024;
+  // split form: 48 KB of histograms per 256-thread CTA lets four CTAs (32
+  // warps, the register limit at 64 registers) share an SM, which hides the
+  // shared-memory atomic latency of this short per-pair computation (a
+  // 100 KB budget allowed two: 7.6 -> 5.7 ms on the 512^2 x 1024 surface)
+  const size_t budget = o->precision == SS_PREC_FP64 ? 96 * 1024 : 48 * 1024;
   const size_t per_trace = (size_t)n_seg * elt;
   if (per_trace > 200 * 1024) return SS_ERR_UNSUPPORTED;
   int tb = (int)std::max<size_t>(1, std::min<size_t>(budget / per_trace,
