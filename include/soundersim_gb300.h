@@ -370,16 +370,21 @@ typedef struct {
   double *grad_sigma;        /* (N,) dL/d rms height, or NULL (device) */
   double *grad_alpha;        /* (ss_refracted_adjoint_blocks(N),) partial
                                 sums of dL/d alpha (device; caller adds) */
+  void *scratch;             /* device, ss_refracted_adjoint_scratch_bytes */
+  size_t scratch_bytes;
 } ss_adjoint_io;
 
 int32_t ss_refracted_adjoint_blocks(int32_t n_facets);
+size_t ss_refracted_adjoint_scratch_bytes(int32_t n_traces,
+                                          int32_t n_facets);
 
 /* Gradients of a loss of windowed trace power with respect to per-facet
  * reflectivity (dB; facets->gamma_f64 holds 10^(R/20)), per-facet
  * rms height (facets->sigma) and an attenuation rate alpha scaling the legs
  * of alpha_mask, for the sequential refracted path in coherent mode.
- * Recomputes every pair (split form with float64 lookup and bin
- * decisions) -- nothing per pair is stored by the forward. Outputs are in
+ * Recomputes every pair in the split form -- nothing per pair is stored by
+ * the forward -- and re-evaluates the few pairs that need a float64 lookup
+ * or bin decision in a fix-up pass (marked in `scratch`). Outputs are in
  * the facet order of the call. */
 int ss_refracted_adjoint(const ss_refracted_opts *opts,
                          const ss_facets *target, const ss_traces *traces,

@@ -102,7 +102,8 @@ class AdjointIO(C.Structure):
     _fields_ = [("field", C.c_void_p), ("grad_power", C.c_void_p),
                 ("bin_lo", C.c_int32), ("bin_hi", C.c_int32),
                 ("alpha_mask", C.c_void_p), ("grad_gamma_db", C.c_void_p),
-                ("grad_sigma", C.c_void_p), ("grad_alpha", C.c_void_p)]
+                ("grad_sigma", C.c_void_p), ("grad_alpha", C.c_void_p),
+                ("scratch", C.c_void_p), ("scratch_bytes", C.c_size_t)]
 
 
 class CoherentJob(C.Structure):
@@ -155,6 +156,8 @@ SIGNATURES = {
                                      C.c_void_p, C.c_void_p, C.c_void_p,
                                      C.c_int32, C.c_void_p, C.c_void_p]),
     "ss_refracted_adjoint_blocks": (C.c_int32, [C.c_int32]),
+    "ss_refracted_adjoint_scratch_bytes": (C.c_size_t, [C.c_int32,
+                                                        C.c_int32]),
     "ss_refracted_adjoint": (C.c_int, [C.POINTER(RefractedOpts),
                                        C.POINTER(Facets), C.POINTER(Traces),
                                        C.POINTER(Pattern),

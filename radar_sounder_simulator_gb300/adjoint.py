@@ -16,10 +16,11 @@ field, P_t = sum_{b in window} |F_t[b]|^2, with
   of ``kernels/coherent.py:131-168``, series of ``roughness.py:127-186``);
 * alpha: attenuation rate (dB/km) of the legs listed in ``alpha_legs``.
 
-Forward: ``ss_refracted_fwd`` (split form). Backward: ``ss_refracted_adjoint``
-recomputes every (trace, facet) phasor from the geometry -- nothing per pair
-is stored -- and returns dL/dR, dL/dsigma and dL/dalpha for the upstream
-dL/dP. Any loss built from P with torch operations (e.g. the squared dB
+Forward: ``ss_refracted_fwd`` (split form, or the FP64 form). Backward:
+``ss_refracted_adjoint`` recomputes every (trace, facet) phasor from the
+geometry -- nothing per pair is stored -- with a fix-up pass for the few
+pairs that need float64 lookup or bin decisions, and returns dL/dR,
+dL/dsigma and dL/dalpha for the upstream dL/dP. Any loss built from P with torch operations (e.g. the squared dB
 misfit of ``db_misfit``) then differentiates end to end.
 """
 
@@ -57,6 +58,7 @@ class WindowPowerModel:
         for leg in self.alpha_legs:
             mask[leg] = 1.0
         self.alpha_mask = np.ascontiguousarray(mask, np.float64)
+        self.scratch = None
         lo, hi = self.window
         if not 0 <= lo < hi <= self.plan.n_seg:
             raise ValueError("window outside [0, n_samples)")
@@ -92,10 +94,15 @@ class WindowPowerModel:
         gA = torch.empty(blocks, dtype=torch.float64, device=self.device)
         gP = grad_power.detach().to(self.device, torch.float64).contiguous()
         field = field.contiguous()
+        nbytes = L.ss_refracted_adjoint_scratch_bytes(self.plan.T, N)
+        if self.scratch is None or self.scratch.numel() < nbytes:
+            self.scratch = torch.empty(nbytes, dtype=torch.uint8,
+                                       device=self.device)
         io = _lib.AdjointIO(field.data_ptr(), gP.data_ptr(), self.window[0],
                             self.window[1],
                             self.alpha_mask.ctypes.data_as(C.c_void_p),
-                            gR.data_ptr(), gS.data_ptr(), gA.data_ptr())
+                            gR.data_ptr(), gS.data_ptr(), gA.data_ptr(),
+                            self.scratch.data_ptr(), nbytes)
         p = self.plan
         stream = torch.cuda.current_stream(self.device).cuda_stream
         st = L.ss_refracted_adjoint(C.byref(p.opts), C.byref(p.fst),

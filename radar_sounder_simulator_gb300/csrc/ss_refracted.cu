@@ -433,6 +433,12 @@ extern "C" int32_t ss_refracted_adjoint_blocks(int32_t n_facets) {
   return n_facets > 0 ? ss::refracted_adjoint_blocks(n_facets) : 0;
 }
 
+extern "C" size_t ss_refracted_adjoint_scratch_bytes(int32_t n_traces,
+                                                     int32_t n_facets) {
+  if (n_traces <= 0 || n_facets <= 0) return 0;
+  return ss::refracted_adjoint_mask_bytes(n_traces, n_facets);
+}
+
 extern "C" int ss_refracted_adjoint(const ss_refracted_opts *opts,
                                     const ss_facets *target,
                                     const ss_traces *traces,
@@ -458,8 +464,14 @@ extern "C" int ss_refracted_adjoint(const ss_refracted_opts *opts,
     set_error("sigma gradients need per-facet rms heights (facets->sigma)");
     return SS_ERR_ARG;
   }
+  if (!io->scratch ||
+      io->scratch_bytes < refracted_adjoint_mask_bytes(a.T, a.N)) {
+    set_error("adjoint scratch buffer too small");
+    return SS_ERR_SCRATCH;
+  }
   AdjArgs j{io->field, io->grad_power, io->bin_lo, io->bin_hi,
-            io->grad_gamma_db, io->grad_sigma, io->grad_alpha};
+            io->grad_gamma_db, io->grad_sigma, io->grad_alpha,
+            static_cast<uint32_t *>(io->scratch)};
   return refracted_adjoint_launch(a, j, io->alpha_mask,
                                   static_cast<cudaStream_t>(stream));
 }

@@ -46,9 +46,11 @@ struct AdjArgs {
   double *grad_gamma_db;     // (N,)
   double *grad_sigma;        // (N,) or null
   double *grad_alpha;        // (refracted_adjoint_blocks(N),) partials
+  uint32_t *defer_mask;      // T x N bits: pairs for the fix-up pass
 };
 
 int refracted_adjoint_blocks(int N);
+size_t refracted_adjoint_mask_bytes(int T, int N);
 int refracted_adjoint_launch(RefArgs &a, const AdjArgs &j,
                              const double *alpha_mask, cudaStream_t st);
 

@@ -12,12 +12,53 @@ namespace ss {
 // over the pairs whose bin lies in the window (bins and paths do not depend
 // on reflectivity, roughness or attenuation). Each pair's contribution c_ti
 // is recomputed from the geometry -- no per-pair state is stored -- with the
-// float64 lookup and bin decisions (EXACT), so the adjoint sees exactly the
-// forward's pairs. Thread <-> facet, loop over all traces (staged in shared
+// forward's lookup and bin decisions: the fast pass holds no float64 code
+// and marks the pairs that need a float64 decision (bit t * N + i of the
+// caller's scratch); the fix-up pass evaluates those with EXACT and adds
+// their terms. Thread <-> facet, loop over all traces (staged in shared
 // memory in blocks), so each facet's gradient is summed by one thread in
 // trace order; the attenuation-rate gradient is reduced per CTA.
 constexpr int kAdjThreads = 128, kAdjTB = 32;
+constexpr double kLn10 = 2.302585092994045684;
 
+// One pair's terms of the three gradients (before the ln10 factors).
+template <int ROUGH, bool EXACT>
+__device__ __forceinline__ bool adjoint_pair(
+    const RefArgs &a, const RefSplitConsts &k, const AdjArgs &j,
+    const TraceS &T, const double *p64, const float *u, const float *pv,
+    const float *pat, int pa_len, const float *lg, const float *fad, int t,
+    int i, const float *q, double g, double &gR, double &gS, double &gA) {
+  PairOut o;
+  PairGrad pg;
+  if (!pair_eval<0, ROUGH, EXACT, true>(a, k, T, p64, u, pv, pat, pa_len, lg,
+                                        fad, i, q, o, &pg))
+    return false;
+  if (o.bin < j.bin_lo || o.bin >= j.bin_hi) return true;
+  const double2 f =
+      reinterpret_cast<const double2 *>(j.field)[(size_t)t * a.n_seg + o.bin];
+  gR += g * (f.x * pg.gre + f.y * pg.gim);
+  gS += g * (f.x * pg.sre + f.y * pg.sim);
+  gA += g * (f.x * o.re + f.y * o.im) * (double)pg.dloss;
+  return true;
+}
+
+template <int ROUGH>
+__device__ __forceinline__ void adjoint_stage_tables(const RefArgs &a,
+                                                     float *s_pat,
+                                                     float *s_fad, float *lg,
+                                                     int &pa_len) {
+  const int tid = threadIdx.x;
+  int pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
+  for (int m = tid; m < pa_len; m += blockDim.x) s_pat[m] = (float)a.pa[m];
+  for (int m = tid; m < pb_len; m += blockDim.x)
+    s_pat[pa_len + m] = (float)a.pb[m];
+  if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
+    s_fad[tid] = (float)a.fad.a[tid];
+  if (ROUGH != SS_ROUGH_NONE)
+    for (int m = tid; m <= a.n_terms; m += blockDim.x)
+      lg[m] = (float)lgamma((double)m + 1.0);
+}
 
 template <int ROUGH>
 __global__ void __launch_bounds__(kAdjThreads)
@@ -36,16 +77,8 @@ refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
   const int i = blockIdx.x * kAdjThreads + tid;
   const int i_first = blockIdx.x * kAdjThreads;
   const int i_last = min(i_first + kAdjThreads, a.N) - 1;
-  int pa_len, pb_len;
-  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
-  for (int m = tid; m < pa_len; m += blockDim.x) s_pat[m] = (float)a.pa[m];
-  for (int m = tid; m < pb_len; m += blockDim.x)
-    s_pat[pa_len + m] = (float)a.pb[m];
-  if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
-    s_fad[tid] = (float)a.fad.a[tid];
-  if (ROUGH != SS_ROUGH_NONE)
-    for (int m = tid; m <= a.n_terms; m += blockDim.x)
-      lg[m] = (float)lgamma((double)m + 1.0);
+  int pa_len;
+  adjoint_stage_tables<ROUGH>(a, s_pat, s_fad, lg, pa_len);
   float q[3] = {0.0f, 0.0f, 0.0f};
   if (i < a.N) {
     q[0] = a.F.cx[i];
@@ -53,7 +86,6 @@ refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
     q[2] = a.F.cz[i];
   }
   double gR = 0.0, gS = 0.0, gA = 0.0;
-  const double2 *F = reinterpret_cast<const double2 *>(j.field);
   for (int t0 = 0; t0 < a.T; t0 += kAdjTB) {
     const int nt = min(kAdjTB, a.T - t0);
     __syncthreads();
@@ -72,26 +104,21 @@ refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
       if (s_hi[tt] <= i_first || s_lo[tt] > i_last || s_g[tt] == 0.0)
         continue;
       if (i >= a.N || i < s_lo[tt] || i >= s_hi[tt]) continue;
-      PairOut o;
-      PairGrad pg;
-      pair_eval<0, ROUGH, true, true>(a, k, s_tr[tt], s_p64[tt], s_u[tt],
-                                      s_pv[tt], s_pat, pa_len, lg, s_fad, i,
-                                      q, o, &pg);
-      if (o.bin < j.bin_lo || o.bin >= j.bin_hi) continue;
-      const double2 f = F[(size_t)(t0 + tt) * a.n_seg + o.bin];
-      const double g = s_g[tt];
-      gR += g * (f.x * pg.gre + f.y * pg.gim);
-      gS += g * (f.x * pg.sre + f.y * pg.sim);
-      gA += g * (f.x * o.re + f.y * o.im) * (double)pg.dloss;
+      if (!adjoint_pair<ROUGH, false>(a, k, j, s_tr[tt], s_p64[tt], s_u[tt],
+                                      s_pv[tt], s_pat, pa_len, lg, s_fad,
+                                      t0 + tt, i, q, s_g[tt], gR, gS, gA)) {
+        const unsigned long long bit =
+            (unsigned long long)(t0 + tt) * a.N + i;
+        atomicOr(&j.defer_mask[bit >> 5], 1u << (bit & 31));
+      }
     }
   }
   // d c / d gamma_dB = c ln(10) / 20; d c / d alpha = -c ln(10) / 10 dloss
-  const double ln10 = 2.302585092994045684;
   if (i < a.N) {
-    j.grad_gamma_db[i] = gR * (ln10 / 20.0);
+    j.grad_gamma_db[i] = gR * (kLn10 / 20.0);
     if (j.grad_sigma) j.grad_sigma[i] = gS;
   }
-  gA *= -ln10 / 10.0;
+  gA *= -kLn10 / 10.0;
   for (int d = 16; d > 0; d >>= 1) gA += __shfl_down_sync(0xffffffffu, gA, d);
   if ((tid & 31) == 0) s_red[tid >> 5] = gA;
   __syncthreads();
@@ -102,8 +129,96 @@ refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
   }
 }
 
+// Fix-up: the deferred pairs with the float64 decisions, added atomically
+// (the fast pass has written every facet's sum). Warp-queued over the
+// bitmask like the forward fix-up.
+template <int ROUGH>
+__global__ void __launch_bounds__(32 * kFixWarps)
+refracted_adjoint_fixup(RefArgs a, RefSplitConsts k, AdjArgs j) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *lg = reinterpret_cast<float *>(smem_raw);
+  __shared__ float s_pat[SS_PAT_MAX];
+  __shared__ float s_fad[SS_FAD_N];
+  __shared__ unsigned long long s_q[kFixWarps][kFixQueue];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int pa_len;
+  adjoint_stage_tables<ROUGH>(a, s_pat, s_fad, lg, pa_len);
+  __syncthreads();
+  const unsigned long long n_words =
+      ((unsigned long long)a.T * a.N + 31) >> 5;
+  const unsigned long long n_warps =
+      (unsigned long long)gridDim.x * kFixWarps;
+  unsigned long long *qv = s_q[warp];
+  auto eval = [&](unsigned long long bit) {
+    const int t = (int)(bit / a.N), i = (int)(bit % a.N);
+    TraceS T;
+    double p64[3];
+    float u[3], pv[6];
+    load_trace(a, t, T, p64, u, pv);
+    const float q[3] = {a.F.cx[i], a.F.cy[i], a.F.cz[i]};
+    double gR = 0.0, gS = 0.0, gA = 0.0;
+    adjoint_pair<ROUGH, true>(a, k, j, T, p64, u, pv, s_pat, pa_len, lg,
+                              s_fad, t, i, q, 2.0 * j.grad_power[t], gR, gS,
+                              gA);
+    if (gR != 0.0) atomicAdd(&j.grad_gamma_db[i], gR * (kLn10 / 20.0));
+    if (gS != 0.0 && j.grad_sigma) atomicAdd(&j.grad_sigma[i], gS);
+    if (gA != 0.0) atomicAdd(&j.grad_alpha[0], gA * (-kLn10 / 10.0));
+  };
+  int qn = 0;
+  for (unsigned long long base =
+           ((unsigned long long)blockIdx.x * kFixWarps + warp) * 32;
+       base < n_words; base += n_warps * 32) {
+    const unsigned long long w = base + lane;
+    unsigned int m = w < n_words ? j.defer_mask[w] : 0u;
+    const int c = __popc(m);
+    int incl = c;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int pos = qn + incl - c;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      qv[pos++] = (w << 5) + b;
+    }
+    __syncwarp();
+    qn += total;
+    while (qn >= 32) {
+      const unsigned long long bit = qv[qn - 32 + lane];
+      __syncwarp();
+      eval(bit);
+      qn -= 32;
+    }
+    __syncwarp();
+  }
+  if (lane < qn) eval(qv[lane]);
+}
+
 int refracted_adjoint_blocks(int N) {
   return (N + kAdjThreads - 1) / kAdjThreads;
+}
+
+size_t refracted_adjoint_mask_bytes(int T, int N) {
+  return (size_t)(((unsigned long long)T * N + 31) / 32) * sizeof(uint32_t);
+}
+
+template <int ROUGH>
+static int adjoint_launch_r(RefArgs &a, const RefSplitConsts &k,
+                            const AdjArgs &j, size_t smem, cudaStream_t st) {
+  const int blocks = refracted_adjoint_blocks(a.N);
+  refracted_adjoint_kernel<ROUGH><<<blocks, kAdjThreads, smem, st>>>(a, k, j);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "refracted adjoint launch");
+  const unsigned long long n_words =
+      ((unsigned long long)a.T * a.N + 31) >> 5;
+  const unsigned long long want =
+      (n_words + 32 * kFixWarps - 1) / (32 * kFixWarps);
+  const int fb = (int)std::max<unsigned long long>(
+      1, std::min<unsigned long long>(want, 8ull * sm_count()));
+  refracted_adjoint_fixup<ROUGH><<<fb, 32 * kFixWarps, smem, st>>>(a, k, j);
+  return cuda_status(cudaGetLastError(), "refracted adjoint fix-up launch");
 }
 
 int refracted_adjoint_launch(RefArgs &a, const AdjArgs &j,
@@ -127,26 +242,19 @@ int refracted_adjoint_launch(RefArgs &a, const AdjArgs &j,
     k.att_mask[m] = alpha_mask ? (float)alpha_mask[m] : 0.0f;
   const size_t smem =
       a.rough_kind ? (size_t)(a.n_terms + 1) * sizeof(float) : 0;
-  const int blocks = refracted_adjoint_blocks(a.N);
+  cudaError_t e = cudaMemsetAsync(
+      j.defer_mask, 0, refracted_adjoint_mask_bytes(a.T, a.N), st);
+  if (e != cudaSuccess) return cuda_status(e, "adjoint mask clear");
   switch (a.rough_kind) {
     case SS_ROUGH_NONE:
-      refracted_adjoint_kernel<SS_ROUGH_NONE>
-          <<<blocks, kAdjThreads, smem, st>>>(a, k, j);
-      break;
+      return adjoint_launch_r<SS_ROUGH_NONE>(a, k, j, smem, st);
     case SS_ROUGH_GAUSS_FULL:
-      refracted_adjoint_kernel<SS_ROUGH_GAUSS_FULL>
-          <<<blocks, kAdjThreads, smem, st>>>(a, k, j);
-      break;
+      return adjoint_launch_r<SS_ROUGH_GAUSS_FULL>(a, k, j, smem, st);
     case SS_ROUGH_GAUSS_AREA:
-      refracted_adjoint_kernel<SS_ROUGH_GAUSS_AREA>
-          <<<blocks, kAdjThreads, smem, st>>>(a, k, j);
-      break;
+      return adjoint_launch_r<SS_ROUGH_GAUSS_AREA>(a, k, j, smem, st);
     default:
-      refracted_adjoint_kernel<SS_ROUGH_EXP_AREA>
-          <<<blocks, kAdjThreads, smem, st>>>(a, k, j);
-      break;
+      return adjoint_launch_r<SS_ROUGH_EXP_AREA>(a, k, j, smem, st);
   }
-  return cuda_status(cudaGetLastError(), "refracted adjoint launch");
 }
 
 }  // namespace ss
