@@ -314,6 +314,14 @@ typedef struct {
 int ss_range_compress(const ss_waveform_opts *opts, const double *taps,
                       const void *in, void *out, void *stream);
 
+/* The same convolution by FFT in float64 (the reference's method,
+ * waveform.py:126-138), for n_samples + n_taps - 1 <= 8192; 0 bytes of
+ * scratch means the size is beyond that (use ss_range_compress). */
+size_t ss_range_compress_fft_scratch_bytes(const ss_waveform_opts *opts);
+int ss_range_compress_fft(const ss_waveform_opts *opts, const double *taps,
+                          const void *in, void *out, void *scratch,
+                          size_t scratch_bytes, void *stream);
+
 /* Frequency-sampled synthesis (Mode F). */
 typedef struct {
   double f0;          /* band centre (Hz) */

@@ -146,6 +146,11 @@ SIGNATURES = {
                                    C.c_void_p]),
     "ss_range_compress": (C.c_int, [C.POINTER(WaveformOpts), C.c_void_p,
                                     C.c_void_p, C.c_void_p, C.c_void_p]),
+    "ss_range_compress_fft_scratch_bytes": (C.c_size_t,
+                                            [C.POINTER(WaveformOpts)]),
+    "ss_range_compress_fft": (C.c_int, [C.POINTER(WaveformOpts), C.c_void_p,
+                                        C.c_void_p, C.c_void_p, C.c_void_p,
+                                        C.c_size_t, C.c_void_p]),
     "ss_multifreq_scratch_bytes": (C.c_size_t, [C.POINTER(MultifreqOpts),
                                                 C.c_int32, C.c_int32]),
     "ss_multifreq_response": (C.c_int, [C.POINTER(MultifreqOpts),

@@ -7,7 +7,9 @@ Same functions and argument meaning as the reference module:
   on the host -- the analytic raised-cosine windowed sinc or the explicit
   LFM matched filter decimated onto the dt lattice;
 * ``convolve_fast_time(arr, kernel, center)`` (waveform.py:126-138) is the
-  'same'-mode fast-time convolution, run by ``ss_range_compress``;
+  'same'-mode fast-time convolution, run by ``ss_range_compress_fft``
+  (float64 FFT, the reference's method) or, beyond 8192 points,
+  ``ss_range_compress`` (compensated direct sum);
 * ``apply_waveform(out, radar, mode)`` (waveform.py:141-160) applies the
   configured waveform: identity for ``kind="delta"``, complex convolution
   in coherent mode, |p|^2 power-envelope convolution in incoherent mode
@@ -72,14 +74,17 @@ def _chirp_pulse(bandwidth, pulse_length, dt, window):
     return p, m
 
 
-def compress_tensor(x, kernel, center, *, power=False, out=None):
+def compress_tensor(x, kernel, center, *, power=False, out=None,
+                    method="auto"):
     """Device form: 'same'-mode convolution of ``x`` along dim 1.
 
     ``x``: CUDA tensor (T, B[, L]) -- complex64/complex128, or float
     (T, B[, L], 2) re/im pairs; with ``power`` a real (T, B[, L]) float
     tensor. ``kernel``: 1-D taps (host array or tensor), zero lag at
     ``center``. Returns complex64 (T, B[, L]) (float32 when ``power``),
-    launched on the current stream.
+    launched on the current stream. ``method``: "fft" (float64 FFT in shared
+    memory, the reference's method; B + len(kernel) - 1 <= 8192), "direct"
+    (compensated direct sum, any size) or "auto" (FFT when it fits).
     """
     if not x.is_cuda:
         raise ValueError("compress_tensor needs a CUDA tensor")
@@ -116,11 +121,25 @@ def compress_tensor(x, kernel, center, *, power=False, out=None):
     o = _lib.WaveformOpts(T, B, L, len(k), int(center), int(bool(power)),
                           int(xr.dtype == torch.float64))
     stream = torch.cuda.current_stream(x.device).cuda_stream
-    st = _lib.lib().ss_range_compress(C.byref(o), C.c_void_p(taps.data_ptr()),
-                                      C.c_void_p(xr.data_ptr()),
-                                      C.c_void_p(out.data_ptr()),
-                                      C.c_void_p(stream))
-    _lib.check(st, "ss_range_compress")
+    L_ = _lib.lib()
+    nfft = L_.ss_range_compress_fft_scratch_bytes(C.byref(o))
+    if method == "fft" and nfft == 0:
+        raise ValueError("B + len(kernel) - 1 above 8192: use the direct sum")
+    if method not in ("auto", "fft", "direct"):
+        raise ValueError(f"unknown method {method!r}")
+    if method != "direct" and nfft > 0:
+        scratch = torch.empty(nfft, dtype=torch.uint8, device=x.device)
+        st = L_.ss_range_compress_fft(
+            C.byref(o), C.c_void_p(taps.data_ptr()),
+            C.c_void_p(xr.data_ptr()), C.c_void_p(out.data_ptr()),
+            C.c_void_p(scratch.data_ptr()), nfft, C.c_void_p(stream))
+        _lib.check(st, "ss_range_compress_fft")
+    else:
+        st = L_.ss_range_compress(C.byref(o), C.c_void_p(taps.data_ptr()),
+                                  C.c_void_p(xr.data_ptr()),
+                                  C.c_void_p(out.data_ptr()),
+                                  C.c_void_p(stream))
+        _lib.check(st, "ss_range_compress")
     return out if power else torch.view_as_complex(out)
 
 

@@ -101,8 +101,50 @@ def test_apply_waveform_incoherent_envelope():
 def test_single_tap_is_identity_and_bad_center_raises():
     import torch
     x = np.random.default_rng(5).normal(size=(2, 300)).astype(np.complex64)
+    # the FFT path (the reference's method) leaves float64 round-off, the
+    # direct sum reproduces the input exactly
     y = wf.convolve_fast_time(x, np.array([1.0]), 0)
-    np.testing.assert_array_equal(y, x.astype(np.complex128))
+    assert np.abs(y - x).max() <= 1e-12 * np.abs(x).max()
+    yd = wf.compress_tensor(torch.as_tensor(x, device="cuda"), np.array([1.0]),
+                            0, method="direct").cpu().numpy()
+    np.testing.assert_array_equal(yd, x)
     xt = torch.zeros((2, 300, 2), dtype=torch.float32, device="cuda")
     with pytest.raises(ValueError):
         wf.compress_tensor(xt, np.ones(3), 3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("method", ["fft", "direct"])
+def test_both_methods_match_the_oracle(method):
+    """FFT (float64, the reference's method) and the compensated direct sum,
+    complex and power-envelope forms, against the float64 oracle."""
+    import torch
+    rng = np.random.default_rng(6)
+    T, B = 3, 900
+    x = (rng.normal(size=(T, B)) + 1j * rng.normal(size=(T, B)))
+    x[:, ::11] *= 1e3
+    x = x.astype(np.complex64)
+    p, m = owf.compressed_pulse(15e6, 8e-6, 1.0 / 30e6, "hann", "chirp")
+    xt = torch.as_tensor(x, device="cuda")
+    y = wf.compress_tensor(xt, p, m, method=method).cpu().numpy()
+    _check(y, owf.convolve_fast_time(x, p, m))
+    pw = (np.abs(x) ** 2).astype(np.float32)
+    yp = wf.compress_tensor(torch.as_tensor(pw, device="cuda"),
+                            np.abs(p) ** 2, m, power=True,
+                            method=method).cpu().numpy()
+    ref = np.maximum(owf.convolve_fast_time(pw, np.abs(p) ** 2, m).real, 0)
+    assert np.abs(yp - ref).max() <= 3e-7 * np.abs(ref).max()
+
+
+@pytest.mark.gpu
+def test_long_rows_fall_back_to_the_direct_sum():
+    import torch
+    rng = np.random.default_rng(7)
+    x = (rng.normal(size=(2, 8000)) +
+         1j * rng.normal(size=(2, 8000))).astype(np.complex64)
+    p, m = owf.compressed_pulse(15e6, 20e-6, 1.0 / 30e6, "hann")
+    xt = torch.as_tensor(x, device="cuda")
+    with pytest.raises(ValueError):
+        wf.compress_tensor(xt, p, m, method="fft")
+    y = wf.compress_tensor(xt, p, m).cpu().numpy()
+    _check(y, owf.convolve_fast_time(x, p, m))
