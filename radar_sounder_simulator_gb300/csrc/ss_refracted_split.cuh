@@ -866,8 +866,12 @@ __device__ __forceinline__ bool pair_eval(
 // Fast kernel: CTA = (facet chunk, trace block); thread <-> facet; per-trace
 // histograms in shared memory; pairs that need a float64 decision are marked
 // in the deferral bitmask (bit t * defer_w + (i - lo_t)).
+// Up to two crossings the solve fits 64 registers, so two 512-thread CTAs
+// share an SM (32 warps; the joint solve through two interfaces spills a
+// few words at that budget and still gains 8%); through three or more it
+// keeps ~125 registers and one CTA.
 template <int NI, int ROUGH, bool PLAIN>
-__global__ void __launch_bounds__(kSplitThreads)
+__global__ void __launch_bounds__(kSplitThreads, NI >= 3 ? 1 : 2)
 refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2 *hist = reinterpret_cast<float2 *>(smem_raw);
