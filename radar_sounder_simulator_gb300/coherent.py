@@ -33,6 +33,15 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
 
 
+def _field_to_host(field, out_dtype):
+    """(T, n, 2) float64 re/im device field -> host complex array; complex64
+    is formed on the device so only half the bytes cross to the host."""
+    if np.dtype(out_dtype) == np.complex64:
+        return torch.view_as_complex(field.to(torch.float32)).cpu().numpy()
+    f = field.cpu().numpy()
+    return (f[..., 0] + 1j * f[..., 1]).astype(out_dtype)
+
+
 class DeviceFacets:
     """Target facets staged on the device in along-track order (SoA)."""
 
@@ -57,14 +66,19 @@ class DeviceFacets:
 
 def stage_facets(centers, normals, areas, e1, e2, order, device, *,
                  gamma=None, sigma=None, corr=None, phasors=None):
-    """Sort, quantise to float32 and upload the facet SoA (one copy)."""
+    """Quantise to float32, upload once and sort into the facet SoA on the
+    device (the along-track permutation is a device gather)."""
     n = len(order)
-    soa = np.empty((13, n), np.float32)
-    soa[0:3] = np.asarray(centers, np.float32)[order].T
-    soa[3:6] = np.asarray(normals, np.float32)[order].T
-    soa[6:9] = np.asarray(e1, np.float32)[order].T
-    soa[9:12] = np.asarray(e2, np.float32)[order].T
-    soa[12] = np.asarray(areas, np.float32)[order]
+    rows = np.empty((n, 13), np.float32)
+    rows[:, 0:3] = centers
+    rows[:, 3:6] = normals
+    rows[:, 6:9] = e1
+    rows[:, 9:12] = e2
+    rows[:, 12] = areas
+    rows_t = torch.from_numpy(rows).to(device)
+    order_t = torch.from_numpy(np.ascontiguousarray(order, np.int64)).to(
+        device)
+    soa = rows_t.index_select(0, order_t).t().contiguous()
     extras = {}
     if gamma is not None:
         extras["gamma_f32"] = _dev(np.asarray(gamma, np.float32)[order],
@@ -78,7 +92,7 @@ def stage_facets(centers, normals, areas, e1, e2, order, device, *,
     if phasors is not None:
         ph = np.asarray(phasors, np.complex64)[order]
         extras["phasor"] = _dev(ph.view(np.float32), np.float32, device)
-    return DeviceFacets(_dev(soa, np.float32, device), extras, n)
+    return DeviceFacets(soa, extras, n)
 
 
 def pattern_struct(pattern, n_traces, device):
@@ -166,8 +180,7 @@ class CoherentPlan:
         return 2
 
     def to_numpy(self, field, dropped, out_dtype=np.complex64):
-        f = field.cpu().numpy()
-        res = (f[..., 0] + 1j * f[..., 1]).astype(out_dtype)
+        res = _field_to_host(field, out_dtype)
         if self.split:
             res = res.reshape(self.T, self.n_samples, 2)
         return res, dropped.cpu().numpy().astype(np.float32)

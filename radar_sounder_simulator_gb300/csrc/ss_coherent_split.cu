@@ -63,16 +63,8 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   const int t_base = group * a.tb;
   const int nt = min(a.tb, a.T - t_base);
   const int tid = threadIdx.x;
-  int pa_len = 0;
-  if (a.pat_kind == SS_PAT_ARRAY || a.pat_kind == SS_PAT_FINITE_DIPOLE)
-    pa_len = 1;
-  else if (a.pat_kind == SS_PAT_ARRAY_TAPERED)
-    pa_len = 2 * a.pat_n;
-  else if (a.pat_kind == SS_PAT_TABULATED)
-    pa_len = a.pat_n;
-  int pb_len = a.pat_kind == SS_PAT_TABULATED ? a.pat_n
-               : (a.pat_kind == SS_PAT_ARRAY ||
-                  a.pat_kind == SS_PAT_ARRAY_TAPERED) ? 4 : 0;
+  int pa_len, pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
 
   if (tid < nt) {
     const int t = t_base + tid;
@@ -389,11 +381,8 @@ SplitConsts coherent_split_consts(const CoArgs &a) {
 }
 
 int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st) {
-  int pa_len = 0, pb_len = 0;
-  if (a.pat_kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
-  if (a.pat_kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
-  if (a.pat_kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * a.pat_n; pb_len = 4; }
-  if (a.pat_kind == SS_PAT_TABULATED) { pa_len = a.pat_n; pb_len = a.pat_n; }
+  int pa_len, pb_len;
+  pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
   if (pa_len + pb_len > SS_PAT_MAX) {
     set_error("antenna table too large for the split kernel");
     return SS_ERR_UNSUPPORTED;

@@ -8,6 +8,18 @@
 namespace ss {
 
 
+// Antenna table lengths (pa, pb) of a pattern kind (antenna.py:76-118
+// packing), staged as floats in shared memory by the split kernels.
+__host__ __device__ __forceinline__ void pattern_lengths(int kind, int n,
+                                                         int &pa_len,
+                                                         int &pb_len) {
+  pa_len = pb_len = 0;
+  if (kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
+  if (kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
+  if (kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * n; pb_len = 4; }
+  if (kind == SS_PAT_TABULATED) { pa_len = n; pb_len = n; }
+}
+
 __device__ __forceinline__ float reduce_2pi(float x) {
   const float n = rintf(x * 0.159154943091895336f);
   float r = __fmaf_rn(-n, 6.28318548202514648f, x);

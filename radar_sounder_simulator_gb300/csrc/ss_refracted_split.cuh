@@ -662,17 +662,6 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   for (int j = 0; j < 3; ++j) P.rh[j] = -seg_last[j].hi * is;
 }
 
-// Antenna table lengths (pa, pb) of a pattern kind.
-__host__ __device__ __forceinline__ void pattern_lengths(int kind, int n,
-                                                         int &pa_len,
-                                                         int &pb_len) {
-  pa_len = pb_len = 0;
-  if (kind == SS_PAT_ARRAY) { pa_len = 1; pb_len = 4; }
-  if (kind == SS_PAT_FINITE_DIPOLE) pa_len = 1;
-  if (kind == SS_PAT_ARRAY_TAPERED) { pa_len = 2 * n; pb_len = 4; }
-  if (kind == SS_PAT_TABULATED) { pa_len = n; pb_len = n; }
-}
-
 // Platform data of trace t in the split kernels' form.
 __device__ __forceinline__ void load_trace(const RefArgs &a, int t, TraceS &T,
                                            double *p64, float *u, float *pv) {

@@ -17,8 +17,29 @@ import numpy as np
 import torch
 
 from . import _lib
-from .coherent import _dev, pattern_struct, rough_struct, stage_facets
+from .coherent import (_dev, _field_to_host, pattern_struct, rough_struct,
+                       stage_facets)
 from .geometry import cull_plan
+
+
+def _affine_fit(x, y, rc):
+    """Least-squares (x, y, 1) -> (row, col) fit, the problem
+    multilayer.py:277-278 hands to lstsq, solved through the 2x2 normal
+    equations of the centred coordinates (well conditioned, O(N), equal to
+    the SVD solution to float64 rounding). Returns coef (3, 2): rows x, y, 1."""
+    mx, my = x.mean(), y.mean()
+    xc, yc = x - mx, y - my
+    sxx, sxy, syy = xc @ xc, xc @ yc, yc @ yc
+    det = sxx * syy - sxy * sxy
+    if not det > 1e-12 * max(sxx * syy, 1e-300):
+        a = np.column_stack([x, y, np.ones(len(x))])
+        return np.linalg.lstsq(a, rc, rcond=None)[0]
+    mr = rc.mean(0)
+    rcc = rc - mr
+    bx, by = xc @ rcc, yc @ rcc
+    cx = (syy * bx - sxy * by) / det
+    cy = (sxx * by - sxy * bx) / det
+    return np.vstack([cx, cy, mr - cx * mx - cy * my])
 
 
 def grid_consts(f):
@@ -30,8 +51,7 @@ def grid_consts(f):
         np.asarray(f.centers).reshape(ny, nx, 3).astype(np.float32),
         np.asarray(f.normals).reshape(ny, nx, 3).astype(np.float32)], -1)
     cen = np.asarray(f.centers, np.float64)
-    a = np.column_stack([cen[:, 0], cen[:, 1], np.ones(len(cen))])
-    coef = np.linalg.lstsq(a, np.asarray(f.cell, np.float64), rcond=None)[0]
+    coef = _affine_fit(cen[:, 0], cen[:, 1], np.asarray(f.cell, np.float64))
     areas = np.asarray(f.areas, np.float64)
     w = (areas / areas.sum())[:, None]
     mp = (cen * w).sum(0)
@@ -98,12 +118,12 @@ class RefractedPlan:
         return 2 if (precision or self.precision) == "fp64" else 3
 
     def to_numpy(self, field, dropped, out_dtype=None):
-        f = field.cpu().numpy()
         if self.coherent:
-            res = (f[..., 0] + 1j * f[..., 1]).astype(out_dtype or
-                                                      np.complex64)
+            res = _field_to_host(field, out_dtype or np.complex64)
         else:
-            res = f[..., 0].astype(out_dtype or np.float32)
+            res = field[..., 0].to(torch.float32 if (out_dtype or np.float32)
+                                   == np.float32 else torch.float64)
+            res = res.cpu().numpy().astype(out_dtype or np.float32)
         if self.split:
             res = res.reshape(self.T, self.n_samples, 2)
         return res, dropped.cpu().numpy().astype(np.float32)

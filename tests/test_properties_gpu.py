@@ -132,3 +132,52 @@ def test_block_size_does_not_change_the_result(precision):
     tol = 1e-12 if precision == "fp64" else 1e-6
     assert np.abs(x - y).max() <= tol * np.abs(x).max()
     np.testing.assert_allclose(dx, dy, rtol=1e-5)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_window_before_every_facet_drops_everything(precision):
+    """No facet bins inside the window: the field is zero and the dropped
+    power is the whole scene's (drop, never wrap)."""
+    c, n, a, e1, e2 = _grid()
+    p = np.array([[5.0, 2.0, 150.0]])
+    k = 2 * np.pi / 5.0
+    kw = dict(k=k, gamma=-0.3, t0=2 * 400.0 / C, dt=2e-9, n_samples=64, c=C,
+              window_cull=False, precision=precision,
+              out_dtype=np.complex128)
+    field, dropped = coherent_cluttergram(p, UCT[None], c, n, a, e1, e2, **kw)
+    assert not np.any(field)
+    q = [np.asarray(v, np.float32).astype(np.float64) for v in (c, n, a, e1,
+                                                               e2)]
+    contrib, _ = lpa.lpa_field(p[0], *q, k, -0.3)
+    np.testing.assert_allclose(dropped[0], (np.abs(contrib) ** 2).sum(),
+                               rtol=1e-5)
+
+
+def test_oversized_window_is_refused_not_truncated():
+    """A per-trace histogram beyond the shared-memory budget is an error
+    (ValueError), never a silently shortened window."""
+    c, n, a, e1, e2 = _grid(ncell=4)
+    p = np.array([[0.0, 0.0, 150.0]])
+    with pytest.raises(ValueError):
+        coherent_cluttergram(p, UCT[None], c, n, a, e1, e2,
+                             k=2 * np.pi / 5.0, gamma=-0.3, t0=0.0, dt=1e-9,
+                             n_samples=40000, c=C, precision="split")
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_ragged_sizes(precision):
+    """Trace and facet counts that are not multiples of any block or tile."""
+    c, n, a, e1, e2 = _grid(ncell=13)
+    rng = np.random.default_rng(23)
+    T = 7
+    p = np.column_stack([rng.uniform(-10, 10, T), rng.uniform(-10, 10, T),
+                         rng.uniform(140, 160, T)])
+    kw = dict(k=2 * np.pi / 5.0, gamma=-0.3, t0=2 * 130.0 / C, dt=2e-9,
+              n_samples=77, c=C, block_size=17)
+    got, _ = coherent_cluttergram(p, np.tile(UCT, (T, 1)), c, n, a, e1, e2,
+                                  **kw, precision=precision,
+                                  out_dtype=np.complex128)
+    ref, _ = lpa.coherent_cluttergram(p, np.tile(UCT, (T, 1)), c, n, a, e1,
+                                      e2, **kw)
+    tol = 1e-9 if precision == "fp64" else 1e-4
+    assert np.linalg.norm(got - ref) <= tol * np.linalg.norm(ref)
