@@ -414,7 +414,7 @@ def main():
                                         os.cpu_count() or 1)
             cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1,
                    "kind": "port", "sample": sample}
-        rows = run_rows(args, device) if ws == 1 else None
+        rows = run_rows(args, device, peak) if ws == 1 else None
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup,
                 "ms_per_step": ms, "higher_is_better": True,
@@ -476,7 +476,14 @@ def _errors(a, b):
     return {"rel_l2": rel, "phase_rad": ph, "power_db": db}
 
 
-def row_cfg1(device, flush):
+def _roof(flop, ms, peak, bound, per_unit, note):
+    achieved = flop / (ms * 1e-3) / 1e12
+    return {"bound": bound, "achieved": achieved, "peak": peak,
+            "unit": "TFLOP/s", "frac": achieved / peak,
+            "flop_per_unit": per_unit, "ms": ms, "note": note}
+
+
+def row_cfg1(device, flush, peaks):
     """Plain surface, delta-binned coherent sum + LFM pulse compression."""
     from radar_sounder_simulator_gb300 import scenes
     from radar_sounder_simulator_gb300.coherent import prepare_coherent
@@ -496,20 +503,30 @@ def row_cfg1(device, flush):
         out[prec] = compress_tensor(fld, pulse, m)
     ms = _events_ms(lambda: step("split"), 5, flush)
     ms64 = _events_ms(lambda: step("fp64"), 2, flush)
+    ms_k = _events_ms(lambda: pl["split"].run(), 5, flush)
     fld, _ = pl["split"].run()
     ms_rc = _events_ms(lambda: compress_tensor(fld, pulse, m), 5, flush)
     pairs = len(f.centers) * len(cfg.pos)
     T, B = len(cfg.pos), cfg.kw["n_samples"]
+    n_fft = 1 << int(np.ceil(np.log2(B + len(pulse) - 1)))
+    fft_flop = 2 * 5.0 * n_fft * np.log2(n_fft) + 6.0 * n_fft
     return {"workload": "surface_128sq_100m_256tr_2048bins_chirp_20us",
             "unit": "contribs/s", "value": pairs / (ms * 1e-3),
             "ms_per_step": ms, "fp64_value": pairs / (ms64 * 1e-3),
             "split_over_fp64": ms64 / ms,
-            "range_compression": {"taps": len(pulse), "ms": ms_rc,
-                                  "samples_per_s": T * B / (ms_rc * 1e-3)},
+            "roofline": _roof(pairs * 47.0, ms_k, peaks["fp32"], "fp32", 47.0,
+                              "surface facet sum (main pass + reduce), 47 "
+                              "FLOP per smooth isotropic pair"),
+            "range_compression": {
+                "taps": len(pulse), "ms": ms_rc, "method": "fft",
+                "samples_per_s": T * B / (ms_rc * 1e-3),
+                "roofline": _roof(T * fft_flop, ms_rc, peaks["fp64"], "fp64",
+                                  fft_flop, f"float64 FFT convolution per "
+                                  f"row: 2 x 5 N log2 N + 6 N, N = {n_fft}")},
             "error_vs_fp64": _errors(out["split"], out["fp64"])}
 
 
-def row_modef(device, flush):
+def row_modef(device, flush, peaks):
     """Frequency-sampled synthesis of the config-1 scene, K = 1024."""
     from radar_sounder_simulator_gb300 import scenes
     from radar_sounder_simulator_gb300.multifreq import prepare_multifreq
@@ -525,12 +542,18 @@ def row_modef(device, flush):
                                precision=prec, device=device)
         ms[prec] = _events_ms(pl.run, 3 if prec == "split" else 1, flush)
         res[prec] = _complex(pl.run())
+        if prec == "split":
+            ms_resp = _events_ms(pl.response, 3, flush)
     units = len(f.centers) * len(cfg.pos) * 1024
     return {"workload": "surface_128sq_100m_256tr_K1024_frozen",
             "unit": "pair-frequencies/s", "value": units / (ms["split"] * 1e-3),
             "ms_per_step": ms["split"],
             "fp64_value": units / (ms["fp64"] * 1e-3),
             "split_over_fp64": ms["fp64"] / ms["split"],
+            "roofline": _roof(units * 8.0, ms_resp, peaks["fp32"], "fp32",
+                              8.0, "band response (main pass + reduce), 8 "
+                              "FLOP per pair-frequency (complex rotate and "
+                              "accumulate, frozen amplitudes)"),
             "error_vs_fp64": _errors(res["split"], res["fp64"])}
 
 
@@ -590,7 +613,7 @@ def row_cfg3(device, flush):
             "ms_per_step": total_ms, "bands": bands}
 
 
-def row_cfg4(device, n_inst, flush):
+def row_cfg4(device, n_inst, flush, peaks):
     """Batched design sweep: one persistent work-queue launch over all
     instances, captured in a CUDA graph, autotuned decomposition."""
     import torch
@@ -640,6 +663,9 @@ def row_cfg4(device, n_inst, flush):
     return {"workload": f"design_sweep_{n_inst}_instances",
             "unit": "contribs/s", "value": pairs / (ms * 1e-3),
             "ms_per_step": ms, "pairs": pairs, "launches_per_step": 2,
+            "roofline": _roof(pairs * 57.0, ms, peaks["fp32"], "fp32", 57.0,
+                              "persistent kernel + batched reduce, 47 FLOP "
+                              "per pair + 10 for the tabulated antenna"),
             "cuda_graph": True, "tuning": list(tun),
             "host_prep_s": host_s,
             "fp64_subset": {"instances": len(plans64),
@@ -695,15 +721,21 @@ def row_cfg5(device, flush):
                            "alpha": float(a.grad)}}
 
 
-def run_rows(args, device):
+def run_rows(args, device, peak32):
     import torch
     want = [] if args.rows == "none" else args.rows.split(",")
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
     rows = {}
-    fns = {"cfg1": lambda: row_cfg1(device, flush),
-           "modef": lambda: row_modef(device, flush),
+    if not want:
+        return rows
+    peaks = {"fp32": peak32, "fp64": fp32_peak_tflops(device, fp64=True)}
+    rows["peaks_tflops"] = {**peaks, "source": "FMA probes measured in this "
+                            "run (ss_fp32_fma_probe, ss_fp64_fma_probe)"}
+    fns = {"cfg1": lambda: row_cfg1(device, flush, peaks),
+           "modef": lambda: row_modef(device, flush, peaks),
            "cfg3": lambda: row_cfg3(device, flush),
-           "cfg4": lambda: row_cfg4(device, args.batch_instances, flush),
+           "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,
+                                    peaks),
            "cfg5": lambda: row_cfg5(device, flush)}
     for name in want:
         t0 = time.perf_counter()
@@ -714,7 +746,6 @@ def run_rows(args, device):
         rows[name]["wall_s"] = time.perf_counter() - t0
         torch.cuda.empty_cache()
     return rows
-
 
 
 def split_error(outs, outs64):
@@ -772,23 +803,23 @@ def pair_flops(n_crossed, joint):
 LAYER_PATHS = [(0, False), (1, False), (2, True), (3, True)]
 
 
-def fp32_peak_tflops(device, repeats=5):
-    """FP32 FMA rate of this GPU, measured with the library's probe kernel
-    (best of ``repeats`` launches, TFLOP/s)."""
+def fp32_peak_tflops(device, repeats=5, fp64=False):
+    """FP32 (or FP64) FMA rate of this GPU, measured with the library's
+    probe kernel (best of ``repeats`` launches, TFLOP/s)."""
     import ctypes as C
     import torch
     from radar_sounder_simulator_gb300 import _lib
     sms = torch.cuda.get_device_properties(device).multi_processor_count
-    blocks, iters = 8 * sms, 40000
-    out = torch.empty(blocks * 256, dtype=torch.float32, device=device)
+    blocks, iters = 8 * sms, (1000 if fp64 else 40000)
+    out = torch.empty(blocks * 256, dtype=torch.float64 if fp64 else
+                      torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
     L = _lib.lib()
+    probe = L.ss_fp64_fma_probe if fp64 else L.ss_fp32_fma_probe
 
     def launch():
-        _lib.check(L.ss_fp32_fma_probe(blocks, iters,
-                                       C.c_void_p(out.data_ptr()),
-                                       C.c_void_p(stream.cuda_stream)),
-                   "ss_fp32_fma_probe")
+        _lib.check(probe(blocks, iters, C.c_void_p(out.data_ptr()),
+                         C.c_void_p(stream.cuda_stream)), "fma probe")
     for _ in range(3):
         launch()
     best = 0.0

@@ -366,6 +366,11 @@ int ss_multifreq_synth(const ss_multifreq_opts *opts, int32_t n_traces,
 int ss_fp32_fma_probe(int32_t blocks, int32_t iters, float *out,
                       void *stream);
 
+/* FP64 twin of ss_fp32_fma_probe (double chains, `out` blocks * 256
+ * doubles); the roofline denominator of float64-bound kernels. */
+int ss_fp64_fma_probe(int32_t blocks, int32_t iters, double *out,
+                      void *stream);
+
 /* Adjoint of windowed trace power (no counterpart in the reference). */
 typedef struct {
   const double *field;       /* (T, n_samples, 2) forward field of the target

@@ -177,6 +177,8 @@ SIGNATURES = {
                                         C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
+    "ss_fp64_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
+                                    C.c_void_p]),
     "ss_version": (C.c_char_p, []),
     "ss_last_error": (C.c_char_p, []),
 }
