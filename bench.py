@@ -44,7 +44,7 @@ def parse():
                     help="skip the float64-form step and the error check")
     ap.add_argument("--skip-e2e", action="store_true",
                     help="skip the drop-in (host buffers) step")
-    ap.add_argument("--traffic", type=float, default=184.5e6,
+    ap.add_argument("--traffic", type=float, default=188.2e6,
                     help="DRAM bytes per launch of the dominant kernel from "
                          "an ncu capture of the same workload (reported in "
                          "the roofline object; default: the one-pass capture "
