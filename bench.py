@@ -49,7 +49,7 @@ def parse():
                          "an ncu capture of the same workload (reported in "
                          "the roofline object; default: the one-pass capture "
                          "of the bed launch at the default size)")
-    ap.add_argument("--rows", default="cfg1,modef,cfg3,cfg4,cfg5",
+    ap.add_argument("--rows", default="cfg1,modef,cfg3,cfg4,cfg5,incoh",
                     help="secondary workloads measured after the headline "
                          "(comma list, or 'none')")
     ap.add_argument("--batch-instances", type=int, default=96)
@@ -721,6 +721,27 @@ def row_cfg5(device, flush):
                            "alpha": float(a.grad)}}
 
 
+def row_incoh(device, flush, peaks):
+    """Incoherent (power) facet sum of the multilayer scene's surface: every
+    facet for every trace, as the reference's incoherent kernel does."""
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.incoherent import prepare_incoherent
+    cfg = scenes.config2()
+    f = cfg.layers[0]
+    pl = prepare_incoherent(cfg.pos, cfg.uct, f.centers, f.normals, f.areas,
+                            t0=cfg.t0, dt=cfg.dt, n_samples=cfg.n_samples,
+                            c=cfg.c, device=device)
+    ms = _events_ms(pl.run, 5, flush)
+    pairs = len(f.centers) * len(cfg.pos)
+    return {"workload": "surface_512sq_50m_1024tr_20km_2048bins_incoherent",
+            "unit": "contribs/s", "value": pairs / (ms * 1e-3),
+            "ms_per_step": ms,
+            "roofline": _roof(pairs * 25.0, ms, peaks["fp32"], "fp32", 25.0,
+                              "incoherent facet sum (main pass + reduce), 25 "
+                              "FLOP per pair: range 9, incidence 6, power 5, "
+                              "bin 5")}
+
+
 def run_rows(args, device, peak32):
     import torch
     want = [] if args.rows == "none" else args.rows.split(",")
@@ -736,7 +757,8 @@ def run_rows(args, device, peak32):
            "cfg3": lambda: row_cfg3(device, flush),
            "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,
                                     peaks),
-           "cfg5": lambda: row_cfg5(device, flush)}
+           "cfg5": lambda: row_cfg5(device, flush),
+           "incoh": lambda: row_incoh(device, flush, peaks)}
     for name in want:
         t0 = time.perf_counter()
         try:

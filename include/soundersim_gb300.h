@@ -245,6 +245,41 @@ int ss_refracted_fwd(const ss_refracted_opts *opts, const ss_facets *target,
                      const ss_roughness *rough, const ss_output *out,
                      void *scratch, size_t scratch_bytes, void *stream);
 
+/* ---- incoherent (power) facet sum ------------------------------------ */
+
+/* Incoherent kernel options (kernels/incoherent.py:64-66 keywords). The
+ * window scalars are rounded to float32 inside, as the reference does
+ * (incoherent.py:101-102). block_size has no counterpart: it only groups the
+ * reference's float32 sums. */
+typedef struct {
+  double t0, dt, c;
+  int32_t n_samples;
+  int32_t split_sides;
+} ss_incoherent_opts;
+
+/* float32 outputs, the reference's return types (incoherent.py:96-103). */
+typedef struct {
+  float *power;    /* (device) (T, n_samples) or (T, n_samples, 2)
+                      [left, right]                                        */
+  float *dropped;  /* (device) (T,) out-of-window power                    */
+} ss_incoherent_output;
+
+size_t ss_incoherent_scratch_bytes(const ss_incoherent_opts *opts,
+                                   int32_t n_traces, int32_t n_facets);
+
+/* Binned incoherent power (A cos)^2 / r^4, times g^4 with a pattern, of
+ * every facet for every trace (no culling, like the reference). Replaces the
+ * jitted vmap(one_trace) program of kernels/incoherent.py:32-61
+ * (`_incoherent_fn`), called at kernels/incoherent.py:100-103. Uses
+ * facets->cx..nz and area only (float32), traces->pos, ->uct (split_sides)
+ * and ->pv (pattern); traces->off is ignored. Bins equal the reference's
+ * float32 bins bit for bit; powers are float32 sums (chunk partials added
+ * in float64). */
+int ss_incoherent_fwd(const ss_incoherent_opts *opts, const ss_facets *facets,
+                      const ss_traces *traces, const ss_pattern *pattern,
+                      const ss_incoherent_output *out, void *scratch,
+                      size_t scratch_bytes, void *stream);
+
 /* Batched surface coherent sums (no counterpart in the reference, which
  * calls coherent_cluttergram once per scene): one job per call of
  * ss_coherent_fwd, all jobs of a batch with the same precision and

@@ -117,6 +117,15 @@ class BatchTuning(C.Structure):
                 ("items_per_sm", C.c_int32), ("ctas_per_sm", C.c_int32)]
 
 
+class IncoherentOpts(C.Structure):
+    _fields_ = [("t0", C.c_double), ("dt", C.c_double), ("c", C.c_double),
+                ("n_samples", C.c_int32), ("split_sides", C.c_int32)]
+
+
+class IncoherentOutput(C.Structure):
+    _fields_ = [("power", C.c_void_p), ("dropped", C.c_void_p)]
+
+
 class BatchInfo(C.Structure):
     _fields_ = [("n_jobs", C.c_int32), ("precision", C.c_int32),
                 ("rough_kind", C.c_int32), ("threads", C.c_int32),
@@ -175,6 +184,13 @@ SIGNATURES = {
         C.c_void_p, C.c_size_t, C.POINTER(BatchInfo)]),
     "ss_coherent_batch_run": (C.c_int, [C.POINTER(BatchInfo), C.c_void_p,
                                         C.c_void_p]),
+    "ss_incoherent_scratch_bytes": (C.c_size_t, [C.POINTER(IncoherentOpts),
+                                                 C.c_int32, C.c_int32]),
+    "ss_incoherent_fwd": (C.c_int, [C.POINTER(IncoherentOpts),
+                                    C.POINTER(Facets), C.POINTER(Traces),
+                                    C.POINTER(Pattern),
+                                    C.POINTER(IncoherentOutput), C.c_void_p,
+                                    C.c_size_t, C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
     "ss_fp64_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,

@@ -1,6 +1,6 @@
 """Freeze the reference's own outputs as golden fixtures (run here, once).
 
-    PYTHONPATH=. python tests/golden/make_golden.py [/path/to/reference]
+    PYTHONPATH=. python tests/golden/make_golden.py [--only a,b] [/path/to/reference]
 
 Runs the UNMODIFIED soundersim source (``refload`` + ``jaxshim``: NumPy in
 place of JAX) on small seeded scenes and writes ``tests/golden/*.npz``.
@@ -317,16 +317,68 @@ def make_waveform(ns):
     return out
 
 
+def make_incoherent(ns):
+    """incoherent_cluttergram (kernels/incoherent.py:58-103), float32 by
+    design: isotropic, split sides, dipole pattern, small blocks."""
+    out = {}
+    F = ns.Facets
+    surf = grid_scene(F, 32, 25.0, 0.0, 1.5, seed=31, slope=(0.01, 0.02))
+    out.update(facet_dict("surf", surf))
+    p, u = track(9, 1200.0, 35.0)
+    out.update(pos=p, uct=u)
+    r = np.linalg.norm(p[:, None, :] - surf.centers[None], axis=-1)
+    # the window starts after the nearest facets and ends before the
+    # farthest, so both ends drop power
+    t0 = 2 * (r.min() + 4.0) / C
+    dt, n_s = 2.5e-8, 40
+    out.update(t0=t0, dt=dt, n_samples=n_s)
+    inc = refload.importlib.import_module("soundersim.kernels.incoherent")
+    # per-pair float32 bins through the reference's own geometry helpers
+    # (the calls incoherent.py:42 and :47 make)
+    f32 = np.float32
+    b = [ns.geometry.twtt_bin(
+        f32(2.0) * ns.geometry.ranges_and_cos(
+            p[t].astype(f32), surf.centers.astype(f32),
+            surf.normals.astype(f32))[0] / f32(C), f32(t0), f32(dt))
+        for t in range(len(p))]
+    out["inc_pair_bins"] = np.stack(b).astype(np.int32)
+    ns_cfg = refload.importlib.import_module("soundersim.config")
+    kind, pv, pa, pb = ns.antenna.pattern_args(
+        ns_cfg.AntennaConfig(kind="dipole", axis="cross_track"),
+        np.tile([1.0, 0, 0], (len(p), 1)), u)
+    out.update(ant_kind=np.array(kind), ant_pv=pv,
+               ant_pa=np.asarray(pa, np.float64),
+               ant_pb=np.asarray(pb, np.float64))
+    base = dict(t0=t0, dt=dt, n_samples=n_s, c=C)
+    cases = {"iso": dict(), "split": dict(split_sides=True),
+             "dipole": dict(pattern=(kind, pv, pa, pb)),
+             "blocks": dict(block_size=100)}
+    for name, kw in cases.items():
+        pw, drp = inc.incoherent_cluttergram(p, u, surf.centers, surf.normals,
+                                             surf.areas, **{**base, **kw})
+        out[f"inc_{name}_power"] = np.asarray(pw)
+        out[f"inc_{name}_dropped"] = np.asarray(drp)
+    return out
+
+
 def main():
-    if len(sys.argv) > 1:
-        os.environ["SOUNDERSIM_REF"] = sys.argv[1]
-        refload.REF_ROOT = sys.argv[1]
-        refload.SRC = os.path.join(sys.argv[1], "src", "soundersim")
+    only = None
+    args = [a for a in sys.argv[1:]]
+    if args and args[0] == "--only":
+        only = set(args[1].split(","))
+        args = args[2:]
+    if args:
+        os.environ["SOUNDERSIM_REF"] = args[0]
+        refload.REF_ROOT = args[0]
+        refload.SRC = os.path.join(args[0], "src", "soundersim")
     ns = refload.load()
     for name, fn in (("primitives", make_primitives), ("antenna", make_antenna),
                      ("coherent", make_coherent),
                      ("refracted", make_refracted),
-                     ("waveform", make_waveform)):
+                     ("waveform", make_waveform),
+                     ("incoherent", make_incoherent)):
+        if only is not None and name not in only:
+            continue
         data = fn(ns)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **data)
