@@ -49,7 +49,7 @@ def parse():
                          "an ncu capture of the same workload (reported in "
                          "the roofline object; default: the one-pass capture "
                          "of the bed launch at the default size)")
-    ap.add_argument("--rows", default="cfg1,modef,cfg3,cfg4,cfg5,incoh",
+    ap.add_argument("--rows", default="cfg1,modef,cfg3,cfg4,cfg5,incoh,focus",
                     help="secondary workloads measured after the headline "
                          "(comma list, or 'none')")
     ap.add_argument("--batch-instances", type=int, default=96)
@@ -742,6 +742,45 @@ def row_incoh(device, flush, peaks):
                               "bin 5")}
 
 
+def row_focus(device, flush, peaks):
+    """Focused SAR (time-domain backprojection) of a 1024-trace, 2048-bin
+    line at 20 km, 25 m spacing, 60 MHz, 1.9 km hann aperture."""
+    import torch
+    from radar_sounder_simulator_gb300.processing import (along_track,
+                                                          focus_tensor)
+    rng = np.random.default_rng(7)
+    T, nb, lam, dt, ap = 1024, 2048, 299792458.0 / 60e6, 1.0 / 30e6, 1900.0
+    pos = np.column_stack([25.0 * np.arange(T), np.zeros(T),
+                           np.full(T, 20000.0)])
+    twtt = 2 * 19800.0 / 299792458.0 + np.arange(nb) * dt
+    F = (rng.standard_normal((T, nb)) + 1j * rng.standard_normal((T, nb))
+         ).astype(np.complex64)
+    ft = torch.as_tensor(F, device=device)
+    tw = torch.as_tensor(twtt, device=device)
+    s = along_track(pos)
+    st = torch.as_tensor(s, device=device)
+    n_terms = int(sum(np.count_nonzero(np.abs(s - si) <= ap / 2)
+                      for si in s)) * nb
+    res, ms = {}, {}
+    for prec in ("split", "fp64"):
+        def run():
+            return focus_tensor(ft, tw, st, wavelength=lam, aperture_m=ap,
+                                precision=prec, out_dtype=torch.complex128)
+        ms[prec] = _events_ms(run, 5 if prec == "split" else 2, flush)
+        res[prec] = run()[0]
+    return {"workload": "focus_1024tr_2048bins_20km_25m_1900m_hann",
+            "unit": "terms/s", "value": n_terms / (ms["split"] * 1e-3),
+            "terms": n_terms, "ms_per_step": ms["split"],
+            "fp64_value": n_terms / (ms["fp64"] * 1e-3),
+            "split_over_fp64": ms["fp64"] / ms["split"],
+            "roofline": _roof(n_terms * 33.0, ms["split"], peaks["fp32"],
+                              "fp32", 33.0, "backprojection (bounds + main "
+                              "pass), 33 FLOP per aperture term: delay 12, "
+                              "interpolation 9, phase 4, weight and "
+                              "accumulate 8"),
+            "error_vs_fp64": _errors(res["split"], res["fp64"])}
+
+
 def run_rows(args, device, peak32):
     import torch
     want = [] if args.rows == "none" else args.rows.split(",")
@@ -758,7 +797,8 @@ def run_rows(args, device, peak32):
            "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,
                                     peaks),
            "cfg5": lambda: row_cfg5(device, flush),
-           "incoh": lambda: row_incoh(device, flush, peaks)}
+           "incoh": lambda: row_incoh(device, flush, peaks),
+           "focus": lambda: row_focus(device, flush, peaks)}
     for name in want:
         t0 = time.perf_counter()
         try:

@@ -280,6 +280,43 @@ int ss_incoherent_fwd(const ss_incoherent_opts *opts, const ss_facets *facets,
                       const ss_incoherent_output *out, void *scratch,
                       size_t scratch_bytes, void *stream);
 
+/* ---- focused SAR (time-domain backprojection) ------------------------ */
+
+#define SS_WIN_HANN 0  /* 0.5 (1 + cos(pi d / (L/2))) */
+#define SS_WIN_RECT 1  /* rectangular ("none")        */
+
+/* processing.py:262-348 focused_sar arguments, on plain arrays. */
+typedef struct {
+  double wavelength;   /* carrier wavelength (m): k = 2 pi / wavelength     */
+  double aperture_m;   /* full aperture L; traces with |s_j - s_i| <= L/2   */
+  double c;            /* wave speed of the twtt -> range map (air)         */
+  int32_t n_traces;    /* T */
+  int32_t n_bins;      /* nb >= 2: t0 = twtt[0], dt = twtt[1] - twtt[0]     */
+  int32_t window;      /* SS_WIN_*                                          */
+  int32_t precision;   /* SS_PREC_FP64 (the reference's float64 chain) or
+                          SS_PREC_SPLIT (float32 arithmetic)                */
+  int32_t in_f64;      /* field elements: 1 complex128, 0 complex64         */
+} ss_focus_opts;
+
+/* Any subset may be NULL (at least one set); layout (T, nb). */
+typedef struct {
+  double *field_c128;  /* (device) complex128 interleaved                   */
+  float *field_c64;    /* (device) complex64 interleaved                    */
+  float *power;        /* (device) float32 |out|^2 (processing.py:345)      */
+} ss_focus_output;
+
+/* Scratch for the per-trace aperture bounds (8 bytes per trace). */
+size_t ss_focused_sar_scratch_bytes(const ss_focus_opts *opts);
+
+/* Focused field of every trace: replaces the loop of processing.py:317-329.
+ * field (device) (T, nb) complex, twtt (device) (nb,) float64 fast-time
+ * axis, s (device) (T,) float64 along-track arc length, non-decreasing
+ * (processing.py:65-69 computes it from the positions). */
+int ss_focused_sar(const ss_focus_opts *opts, const void *field,
+                   const double *twtt, const double *s,
+                   const ss_focus_output *out, void *scratch,
+                   size_t scratch_bytes, void *stream);
+
 /* Batched surface coherent sums (no counterpart in the reference, which
  * calls coherent_cluttergram once per scene): one job per call of
  * ss_coherent_fwd, all jobs of a batch with the same precision and

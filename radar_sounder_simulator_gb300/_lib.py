@@ -16,6 +16,7 @@ PREC = {"fp64": 0, "split": 1}
 PATTERN = {"isotropic": 0, "dipole": 1, "array": 2, "array_tapered": 3,
            "finite_dipole": 4, "tabulated": 5}
 ROUGH_NONE, ROUGH_GAUSS_FULL, ROUGH_GAUSS_AREA, ROUGH_EXP_AREA = range(4)
+WIN_HANN, WIN_RECT = range(2)
 
 _f = C.POINTER(C.c_float)
 _d = C.POINTER(C.c_double)
@@ -126,6 +127,18 @@ class IncoherentOutput(C.Structure):
     _fields_ = [("power", C.c_void_p), ("dropped", C.c_void_p)]
 
 
+class FocusOpts(C.Structure):
+    _fields_ = [("wavelength", C.c_double), ("aperture_m", C.c_double),
+                ("c", C.c_double), ("n_traces", C.c_int32),
+                ("n_bins", C.c_int32), ("window", C.c_int32),
+                ("precision", C.c_int32), ("in_f64", C.c_int32)]
+
+
+class FocusOutput(C.Structure):
+    _fields_ = [("field_c128", C.c_void_p), ("field_c64", C.c_void_p),
+                ("power", C.c_void_p)]
+
+
 class BatchInfo(C.Structure):
     _fields_ = [("n_jobs", C.c_int32), ("precision", C.c_int32),
                 ("rough_kind", C.c_int32), ("threads", C.c_int32),
@@ -191,6 +204,11 @@ SIGNATURES = {
                                     C.POINTER(Pattern),
                                     C.POINTER(IncoherentOutput), C.c_void_p,
                                     C.c_size_t, C.c_void_p]),
+    "ss_focused_sar_scratch_bytes": (C.c_size_t, [C.POINTER(FocusOpts)]),
+    "ss_focused_sar": (C.c_int, [C.POINTER(FocusOpts), C.c_void_p,
+                                 C.c_void_p, C.c_void_p,
+                                 C.POINTER(FocusOutput), C.c_void_p,
+                                 C.c_size_t, C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
     "ss_fp64_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,

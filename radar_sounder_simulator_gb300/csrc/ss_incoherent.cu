@@ -11,10 +11,10 @@
 // that must match the reference's float32 chain
 //   r = sqrt((dx^2 + dy^2) + dz^2), tw = (2 r) / c, u = (tw - t0) / dt
 // bit for bit, with each operation rounded to nearest. The kernel evaluates
-// it first with a MUFU reciprocal square root and reciprocal multiplies and
-// an error bound; only pairs whose fast value lies within that bound of an
-// integer re-run the exactly rounded chain (__fsqrt_rn / __fdiv_rn), so the
-// bins equal the reference's while the common case costs a few instructions.
+// it first as r A - B from a MUFU reciprocal square root, with an error
+// bound; only pairs whose fast value lies within that bound of an integer
+// re-run the exactly rounded chain (__fsqrt_rn / __fdiv_rn), so the bins
+// equal the reference's while the common case costs a few instructions.
 //
 // Work decomposition: the grid is (facet chunks) x (trace blocks of TB
 // traces). Each thread takes one facet at a time and evaluates it against
@@ -35,7 +35,8 @@ struct IncArgs {
   const float *cx, *cy, *cz, *nx, *ny, *nz, *area;
   const double *pos, *uct, *pv;
   int pv_len, T, N, n_samples, n_seg, stride, split;
-  float t0, dt, c, inv_c, inv_dt;
+  float t0, dt, c;  // window scalars rounded to float32
+  float A, B, bandA;  // 2/(c dt), t0/dt, 1e-6 A of those float32 scalars
   int pat_kind, pat_n;
   const double *pa, *pb;
   int n_chunks;
@@ -67,7 +68,10 @@ incoherent_kernel(IncArgs a) {
   if (PAT) pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
 
   if (tid < TB) {
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f), u = p;
+    // missing traces of a short last block get NaN positions: their pairs
+    // fail every comparison, bin nowhere and their dropped sums are unused
+    float4 p = make_float4(__int_as_float(0x7fc00000), 0.f, 0.f, 0.f);
+    float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
     if (tid < nt) {
       const int t = t_base + tid;
       // positions and u_ct rounded to float32 (incoherent.py:86-87)
@@ -93,13 +97,25 @@ incoherent_kernel(IncArgs a) {
   for (int j = tid; j < TB * a.stride; j += blockDim.x) hist[j] = 0.f;
   __syncthreads();
 
+  // step s always pairs this thread with trace (lane + s) mod TB: its
+  // position, histogram row and dropped sum live in registers
+  float px[TB], py[TB], pz[TB], drop[TB];
+  int hoff[TB];
+#pragma unroll
+  for (int s = 0; s < TB; ++s) {
+    const int tt = (lane + s) & (TB - 1);
+    const float4 P = s_p[tt];
+    px[s] = P.x;
+    py[s] = P.y;
+    pz[s] = P.z;
+    hoff[s] = tt * a.stride;
+    drop[s] = 0.f;
+  }
+
   const long len = a.N;
   const int i0 = (int)(len * blockIdx.x / a.n_chunks);
   const int i1 = (int)(len * (blockIdx.x + 1) / a.n_chunks);
   const float nsf = (float)a.n_samples;
-  float drop[TB];
-#pragma unroll
-  for (int s = 0; s < TB; ++s) drop[s] = 0.f;
 
   for (int i = i0 + tid; i < i1; i += blockDim.x) {
     const float cx = a.cx[i], cy = a.cy[i], cz = a.cz[i];
@@ -107,52 +123,48 @@ incoherent_kernel(IncArgs a) {
     const float ar = a.area[i];
 #pragma unroll
     for (int s = 0; s < TB; ++s) {
-      const int tt = (lane + s) & (TB - 1);
-      if (tt >= nt) continue;
-      const float4 P = s_p[tt];
-      const float dx = __fsub_rn(P.x, cx);
-      const float dy = __fsub_rn(P.y, cy);
-      const float dz = __fsub_rn(P.z, cz);
+      const float dx = __fsub_rn(px[s], cx);
+      const float dy = __fsub_rn(py[s], cy);
+      const float dz = __fsub_rn(pz[s], cz);
       const float S = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx),
                                           __fmul_rn(dy, dy)),
                                 __fmul_rn(dz, dz));
       const float y = rsqrtf(S);  // 1/r
-      // power (A cos)^2 / r^4 = (A (d . n))^2 / S^3
-      const float ac = ar * dot3f(dx, dy, dz, nx, ny, nz) * y;
-      const float iS = y * y;
-      float pw = ac * ac * (iS * iS);
+      // power (A cos)^2 / r^4 = (A (d . n))^2 / r^6
+      const float q = ar * dot3f(dx, dy, dz, nx, ny, nz);
+      const float y2 = y * y;
+      float pw = (q * q) * (y2 * y2 * y2);
       if (PAT) {
         // departure direction antenna -> facet (incoherent.py:45)
+        const int tt = (lane + s) & (TB - 1);
         const float g = gain32(a.pat_kind, a.pat_n, pa_len, s_pat, s_pv[tt],
                                -dx * y, -dy * y, -dz * y);
         const float g2 = g * g;
         pw *= g2 * g2;
       }
-      // fast bin and its error bound (bins of twtt, and of u itself)
+      // fast bin u ~ r A - B (A = 2/(c dt), B = t0/dt) and its error bound
+      // |uf - u| <= 4.8e-7 r A + 2.4e-7 |u| (rsqrt 2 ulp, A, B and the
+      // roundings of both chains); the band doubles that. A pair the bound
+      // cannot settle takes the exact chain; a band of half a bin or more
+      // sends every pair there.
       const float rf = S * y;
-      const float twb = (2.0f * rf) * a.inv_c * a.inv_dt;
-      const float uf = __fmaf_rn(2.0f * rf, a.inv_c, -a.t0) * a.inv_dt;
+      const float uf = __fmaf_rn(rf, a.A, -a.B);
       float fb = floorf(uf);
       const float fr = uf - fb;
-      // |uf - u| <= 5.2e-7 tw/dt + 3.6e-7 |u| (rsqrt 2 ulp, reciprocals
-      // and roundings); the band doubles that. A pair whose bin or
-      // in/out-of-window decision the bound cannot settle takes the exact
-      // chain; a band of half a bin or more sends every pair there.
-      const float band = 1e-6f * fabsf(twb) + 7e-7f * fabsf(uf) + 1e-6f;
-      if ((fr < band || fr > 1.0f - band) && uf > -1.0f - band &&
-          uf < nsf + band)
-        fb = bin_exact(S, a);
+      const float band =
+          __fmaf_rn(a.bandA, rf, __fmaf_rn(7e-7f, fabsf(uf), 1e-6f));
+      if (fminf(fr, 1.0f - fr) < band) fb = bin_exact(S, a);
       if (fb >= 0.0f && fb < nsf) {
         int seg = (int)fb;
         if (a.split) {
-          const float4 U = s_u[tt];
+          const float4 U = s_u[(lane + s) & (TB - 1)];
           // (c - p) . u_ct, rounded like the reference's sum
           const float sd = __fadd_rn(__fadd_rn(__fmul_rn(-dx, U.x),
                                                __fmul_rn(-dy, U.y)),
                                      __fmul_rn(-dz, U.z));
           if (sd > 0.0f) seg += a.n_samples;
         }
-        atomicAdd(&hist[tt * a.stride + seg], pw);
+        atomicAdd(&hist[hoff[s] + seg], pw);
       } else {
         drop[s] += pw;
       }
@@ -333,8 +345,9 @@ extern "C" int ss_incoherent_fwd(const ss_incoherent_opts *opts,
   a.t0 = (float)opts->t0;
   a.dt = (float)opts->dt;
   a.c = (float)opts->c;
-  a.inv_c = 1.0f / a.c;
-  a.inv_dt = 1.0f / a.dt;
+  a.A = (float)(2.0 / ((double)a.c * (double)a.dt));
+  a.B = (float)((double)a.t0 / (double)a.dt);
+  a.bandA = 1e-6f * a.A;
   a.pat_kind = kind;
   a.pat_n = pattern ? pattern->n : 0;
   a.pa = pattern ? pattern->pa : nullptr;

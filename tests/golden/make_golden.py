@@ -17,9 +17,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 if __package__ in (None, ""):
     sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
-    from tests.golden import refload  # noqa: E402
+    from tests.golden import refload, xrshim  # noqa: E402
 else:
-    from . import refload
+    from . import refload, xrshim
 
 C = 299792458.0
 
@@ -361,6 +361,58 @@ def make_incoherent(ns):
     return out
 
 
+def focus_scene(T, nb, spacing, z, lam, dt, seed):
+    """Coherent field of three point targets seen from a jittered straight
+    track: per trace a sinc range response at each target's two-way delay
+    with carrier phase exp(-2jkR), plus complex noise."""
+    rng = np.random.default_rng(seed)
+    x = spacing * np.arange(T) + rng.uniform(-0.2, 0.2, T) * spacing
+    pos = np.column_stack([x, 0.3 * np.sin(np.arange(T) / 5.0),
+                           z + 0.5 * np.cos(np.arange(T) / 7.0)])
+    k = 2 * np.pi / lam
+    t0 = 2 * (z - 60.0) / C
+    twtt = t0 + np.arange(nb) * dt
+    targets = np.array([[x[T // 2], 0.0, 0.0], [x[T // 3], 15.0, -20.0],
+                        [x[(3 * T) // 4], -10.0, 12.0]])
+    F = 0.05 * (rng.standard_normal((T, nb)) +
+                1j * rng.standard_normal((T, nb)))
+    for tgt, amp in zip(targets, (1.0, 0.6, 0.8)):
+        R = np.linalg.norm(pos - tgt, axis=1)
+        u = (twtt[None, :] - 2 * R[:, None] / C) / dt
+        F += amp * np.sinc(u) * np.exp(-2j * k * R)[:, None]
+    return pos, twtt, F.astype(np.complex64)
+
+
+def make_focus(ns):
+    """processing.focused_sar (processing.py:262-348) on a small Dataset,
+    through a minimal xarray stand-in; hann and rectangular windows, an
+    aperture of about a dozen traces, a non-uniform along-track spacing."""
+    xr = xrshim.install()
+    proc = refload.importlib.import_module("soundersim.processing")
+    T, nb, lam, dt = 64, 96, 5.0, 1.0 / 30e6
+    pos, twtt, F = focus_scene(T, nb, 8.0, 800.0, lam, dt, seed=41)
+    out = dict(pos=pos, twtt=twtt, field=F, wavelength=lam)
+
+    def dataset():
+        return xr.Dataset(
+            {"field": (("slow_time", "twtt"), F.copy(), {"units": "V"}),
+             "power": (("slow_time", "twtt"), np.abs(F) ** 2, {})},
+            coords={"slow_time": ("slow_time", np.arange(T) * 0.1),
+                    "twtt": ("twtt", twtt.copy()),
+                    "x": ("slow_time", pos[:, 0]),
+                    "y": ("slow_time", pos[:, 1]),
+                    "z": ("slow_time", pos[:, 2])},
+            attrs={"mode": "coherent", "wavelength": lam,
+                   "config": '{"radar": {"c": %r}}' % C})
+    for name, ap, win in (("hann", 96.0, "hann"), ("rect", 96.0, "none"),
+                          ("wide", 250.0, "hann")):
+        res = proc.focused_sar(dataset(), ap, window=win)
+        out[f"focus_{name}_aperture"] = ap
+        out[f"focus_{name}_field"] = np.asarray(res.field.values)
+        out[f"focus_{name}_power"] = np.asarray(res.power.values)
+    return out
+
+
 def main():
     only = None
     args = [a for a in sys.argv[1:]]
@@ -376,7 +428,8 @@ def main():
                      ("coherent", make_coherent),
                      ("refracted", make_refracted),
                      ("waveform", make_waveform),
-                     ("incoherent", make_incoherent)):
+                     ("incoherent", make_incoherent),
+                     ("focus", make_focus)):
         if only is not None and name not in only:
             continue
         data = fn(ns)

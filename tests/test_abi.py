@@ -52,7 +52,9 @@ def test_struct_layouts_match_header(tmp_path):
                "ss_batch_tuning": _lib.BatchTuning,
                "ss_batch_info": _lib.BatchInfo,
                "ss_incoherent_opts": _lib.IncoherentOpts,
-               "ss_incoherent_output": _lib.IncoherentOutput}
+               "ss_incoherent_output": _lib.IncoherentOutput,
+               "ss_focus_opts": _lib.FocusOpts,
+               "ss_focus_output": _lib.FocusOutput}
     lines = ["#include <stdio.h>", "#include <stddef.h>",
              '#include "soundersim_gb300.h"', "int main(void) {"]
     for cname, py in structs.items():
