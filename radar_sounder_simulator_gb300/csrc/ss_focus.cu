@@ -33,6 +33,7 @@ struct FocusArgs {
   const double *twtt;  // (nb,)
   const double *s;     // (T,) along-track arc length
   const int *jr;       // (T, 2) aperture [lo, hi) per output trace
+  float4 *bins;        // (nb,) split form: i00 (as int bits), frac0, r0, -
   int T, nb, window, in_f64;
   double k, c, half;
   ss_focus_output out;
@@ -58,10 +59,8 @@ __device__ __forceinline__ void write_out(const FocusArgs &a, long o,
 
 // Aperture bounds: the contiguous j range with |s_j - s_i| <= half, found
 // with the reference's predicate (float64 difference, then |.| <= half).
-__global__ void focus_bounds_kernel(const double *s, int T, double half,
-                                    int *jr) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= T) return;
+__device__ __forceinline__ void aperture_bounds(const double *s, int T,
+                                                double half, int i, int *jr) {
   const double si = s[i];
   // lo: first j with s_j - s_i >= -half (monotone in j)
   int lo = 0, hi = i + 1;
@@ -100,6 +99,26 @@ __device__ __forceinline__ BinConsts bin_consts(const FocusArgs &a, int b) {
   q.i00 = (int)fl0;
   q.frac0 = __dsub_rn(x0, fl0);
   return q;
+}
+
+// Setup: aperture bounds of every output trace (threads [0, T)) and, for
+// the split form, the per-bin table of float32 constants (threads
+// [T, T + nb)), so the split kernel does no float64 arithmetic per bin.
+__global__ void focus_setup_kernel(FocusArgs a) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < a.T) {
+    aperture_bounds(a.s, a.T, a.half, g, const_cast<int *>(a.jr));
+    return;
+  }
+  const int b = g - a.T;
+  if (a.bins && b < a.nb) {
+    const BinConsts q = bin_consts(a, b);
+    // a fraction just below 1 must not round up to 1.0f: the base index
+    // (and with it the validity of the last bin) is the float64 one
+    a.bins[b] = make_float4(__int_as_float(q.i00),
+                            fminf((float)q.frac0, 0.99999994f), (float)q.r0,
+                            (float)(2.0 / (a.c * q.dt)));
+  }
 }
 
 // hann 0.5 (1 + cos(pi d / half)) (processing.py:315-316), or 1.
@@ -194,10 +213,13 @@ __global__ void __launch_bounds__(256) focus_split_kernel(FocusArgs a) {
   const int b = b0 + tid;
   const int base = b0 - 1;  // the d = 0 sample may sit one bin below b
   const bool live = b < a.nb;
-  const BinConsts q = bin_consts(a, b);
+  // per-bin base index, fraction, r0 and bins per metre of dr
+  const float4 bt = a.bins[live ? b : 0];
+  const int i00 = __float_as_int(bt.x);
+  const float frac0f = bt.y, r0f = bt.z, kx = bt.w;
   const int J0 = a.jr[2 * i0], J1 = a.jr[2 * (i0 + ni - 1) + 1];
   const int nb1 = a.nb - 1;
-  const float kx = (float)(2.0 / (a.c * q.dt));  // bins per metre of dr
+  const float half_f = (float)a.half;
   if (tid == 0) {
     // widest migration of the tile: largest |d| at the nearest bin
     double dmax = 0.0;
@@ -213,12 +235,8 @@ __global__ void __launch_bounds__(256) focus_split_kernel(FocusArgs a) {
     const double h = 258.0 + 4.0 + drm * (double)kx;
     s_W = (int)fmin(h, (double)kFocWMax);
   }
-  const float r0f = (float)q.r0;
   const float r0sq = r0f * r0f;
   const float k2f = (float)(2.0 * a.k);
-  // a fraction just below 1 must not round up to 1.0f: the base index
-  // (and with it the validity of the last bin) is the float64 one
-  const float frac0f = fminf((float)q.frac0, 0.99999994f);
   float accr[kFocTI], acci[kFocTI];
 #pragma unroll
   for (int t = 0; t < kFocTI; ++t) accr[t] = acci[t] = 0.f;
@@ -251,9 +269,10 @@ __global__ void __launch_bounds__(256) focus_split_kernel(FocusArgs a) {
       if (t < ni && r < nr) {
         const int i = i0 + t, j = j0 + r;
         if (j >= a.jr[2 * i] && j < a.jr[2 * i + 1]) {
-          const double dd = __dsub_rn(a.s[j], a.s[i]);
-          d = (float)dd;
-          w = (float)aperture_weight(a, dd);
+          d = (float)__dsub_rn(a.s[j], a.s[i]);
+          w = a.window == SS_WIN_HANN
+                  ? 0.5f * (1.0f + cospif(__fdiv_rn(d, half_f)))
+                  : 1.0f;
         }
       }
       s_d[t][r] = d;
@@ -272,7 +291,7 @@ __global__ void __launch_bounds__(256) focus_split_kernel(FocusArgs a) {
         const float dr = __fdividef(d * d, R + r0f);
         const float xf = __fmaf_rn(dr, kx, frac0f);
         const float fl = floorf(xf);
-        const int ix = q.i00 + (int)fl;
+        const int ix = i00 + (int)fl;
         if ((unsigned)ix >= (unsigned)nb1) continue;
         const float fr = xf - fl;
         const int loc = ix - base;
@@ -312,9 +331,15 @@ __global__ void __launch_bounds__(256) focus_split_kernel(FocusArgs a) {
 
 using namespace ss;
 
+// Scratch: aperture bounds (T, 2) int32, then the (nb,) float4 bin table.
+static size_t focus_bounds_bytes(int T) {
+  return ((size_t)T * 2 * sizeof(int) + 15) & ~(size_t)15;
+}
+
 extern "C" size_t ss_focused_sar_scratch_bytes(const ss_focus_opts *opts) {
-  if (!opts || opts->n_traces <= 0) return 0;
-  return (size_t)opts->n_traces * 2 * sizeof(int);
+  if (!opts || opts->n_traces <= 0 || opts->n_bins <= 0) return 0;
+  return focus_bounds_bytes(opts->n_traces) +
+         (size_t)opts->n_bins * sizeof(float4);
 }
 
 extern "C" int ss_focused_sar(const ss_focus_opts *opts, const void *field,
@@ -343,6 +368,8 @@ extern "C" int ss_focused_sar(const ss_focus_opts *opts, const void *field,
   a.twtt = twtt;
   a.s = s;
   a.jr = reinterpret_cast<int *>(scratch);
+  a.bins = reinterpret_cast<float4 *>(reinterpret_cast<char *>(scratch) +
+                                      focus_bounds_bytes(opts->n_traces));
   a.T = opts->n_traces;
   a.nb = opts->n_bins;
   a.window = opts->window;
@@ -352,9 +379,9 @@ extern "C" int ss_focused_sar(const ss_focus_opts *opts, const void *field,
   a.half = opts->aperture_m / 2.0;
   a.out = *out;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  focus_bounds_kernel<<<(a.T + 255) / 256, 256, 0, st>>>(
-      s, a.T, a.half, const_cast<int *>(a.jr));
-  int e = cuda_status(cudaGetLastError(), "focus bounds launch");
+  const long n_setup = (long)a.T + a.nb;
+  focus_setup_kernel<<<(int)((n_setup + 255) / 256), 256, 0, st>>>(a);
+  int e = cuda_status(cudaGetLastError(), "focus setup launch");
   if (e != SS_OK) return e;
   if ((a.nb + 255) / 256 > 65535) {
     set_error("ss_focused_sar: too many bins");
