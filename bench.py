@@ -733,9 +733,22 @@ def row_incoh(device, flush, peaks):
                             c=cfg.c, device=device)
     ms = _events_ms(pl.run, 5, flush)
     pairs = len(f.centers) * len(cfg.pos)
+    # CPU baseline: the float32 oracle (the reference's algorithm in NumPy)
+    # on 32 traces of the same scene, one core
+    from oracle import incoherent as oinc
+    t0 = time.perf_counter()
+    oinc.incoherent_cluttergram(cfg.pos[:32], cfg.uct[:32], f.centers,
+                                f.normals, f.areas, t0=cfg.t0, dt=cfg.dt,
+                                n_samples=cfg.n_samples, c=cfg.c)
+    cpu_s = time.perf_counter() - t0
     return {"workload": "surface_512sq_50m_1024tr_20km_2048bins_incoherent",
             "unit": "contribs/s", "value": pairs / (ms * 1e-3),
             "ms_per_step": ms,
+            "cpu_baseline": {"value": 32 * len(f.centers) / cpu_s,
+                             "unit": "contribs/s", "cores": 1,
+                             "kind": "port",
+                             "sample": "32 traces x 262144 facets, float32 "
+                                       "NumPy oracle"},
             "roofline": _roof(pairs * 25.0, ms, peaks["fp32"], "fp32", 25.0,
                               "incoherent facet sum (main pass + reduce), 25 "
                               "FLOP per pair: range 9, incidence 6, power 5, "
@@ -768,8 +781,22 @@ def row_focus(device, flush, peaks):
                                 precision=prec, out_dtype=torch.complex128)
         ms[prec] = _events_ms(run, 5 if prec == "split" else 2, flush)
         res[prec] = run()[0]
+    # CPU baseline: the float64 oracle (the reference's loop) on a 96-trace
+    # piece of the line, one core
+    from oracle import processing as oproc
+    Ts = 96
+    s_s = along_track(pos[:Ts])
+    n_cpu = int(sum(np.count_nonzero(np.abs(s_s - si) <= ap / 2)
+                    for si in s_s)) * nb
+    t0 = time.perf_counter()
+    oproc.focused_sar(F[:Ts], twtt, pos[:Ts], lam, ap, "hann")
+    cpu_s = time.perf_counter() - t0
     return {"workload": "focus_1024tr_2048bins_20km_25m_1900m_hann",
             "unit": "terms/s", "value": n_terms / (ms["split"] * 1e-3),
+            "cpu_baseline": {"value": n_cpu / cpu_s, "unit": "terms/s",
+                             "cores": 1, "kind": "port",
+                             "sample": f"{Ts} output traces of the same "
+                                       "line, float64 NumPy oracle"},
             "terms": n_terms, "ms_per_step": ms["split"],
             "fp64_value": n_terms / (ms["fp64"] * 1e-3),
             "split_over_fp64": ms["fp64"] / ms["split"],
