@@ -149,12 +149,13 @@ def host_bytes(cfg):
     h2d = d2h = 0
     for j, f in enumerate(cfg.layers):
         n = len(f.centers)
-        h2d += 13 * 4 * n + 8 * n               # float32 facet rows + order
+        h2d += 13 * 8 * n + 8 * n               # float64 facet arrays + order
         h2d += T * (3 * 8 * 2 + 4)              # positions, u_ct, windows
         if j > 0 and np.ndim(cfg.gammas[j]):
             h2d += 8 * n                        # per-facet gamma
         for g in cfg.layers[:j]:
-            h2d += 6 * 4 * len(g.centers)       # lookup tables
+            h2d += 72 * len(g.centers)          # centres, normals, areas,
+            #                                     cells of crossed interfaces
         d2h += T * cfg.n_samples * 8 + T * 8    # complex64 field + dropped
     return h2d, d2h
 

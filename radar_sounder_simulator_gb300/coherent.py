@@ -33,12 +33,25 @@ def _ptr(t):
     return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
 
 
+def to_host(t):
+    """Device tensor -> NumPy array through a page-locked buffer (the fast
+    device-to-host path; torch caches the page-locked blocks)."""
+    if t.device.type != "cuda":
+        return t.numpy()
+    h = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    h.copy_(t)
+    return h.numpy()
+
+
 def _field_to_host(field, out_dtype):
-    """(T, n, 2) float64 re/im device field -> host complex array; complex64
-    is formed on the device so only half the bytes cross to the host."""
+    """(T, n, 2) float64 re/im device field -> host complex array; the
+    complex dtype is formed on the device so only its bytes cross to the
+    host."""
     if np.dtype(out_dtype) == np.complex64:
-        return torch.view_as_complex(field.to(torch.float32)).cpu().numpy()
-    f = field.cpu().numpy()
+        return to_host(torch.view_as_complex(field.to(torch.float32)))
+    if np.dtype(out_dtype) == np.complex128:
+        return to_host(torch.view_as_complex(field.contiguous()))
+    f = to_host(field)
     return (f[..., 0] + 1j * f[..., 1]).astype(out_dtype)
 
 
@@ -64,34 +77,44 @@ class DeviceFacets:
         return f
 
 
+def permuted(a, dtype, order, device):
+    """``a[order]`` as a device tensor of ``dtype``: gathered on the device
+    when the order is a device tensor, on the host otherwise."""
+    a = np.ascontiguousarray(a, dtype)
+    if isinstance(order, torch.Tensor):
+        return torch.from_numpy(a).to(device).index_select(0, order)
+    return _dev(a[order], dtype, device)
+
+
 def stage_facets(centers, normals, areas, e1, e2, order, device, *,
                  gamma=None, sigma=None, corr=None, phasors=None):
-    """Quantise to float32, upload once and sort into the facet SoA on the
-    device (the along-track permutation is a device gather)."""
+    """Upload the float64 facet arrays as they are and form the float32
+    facet SoA on the device: quantisation, along-track permutation (a
+    gather) and transposition run there, the host does no per-facet
+    arithmetic."""
     n = len(order)
-    rows = np.empty((n, 13), np.float32)
-    rows[:, 0:3] = centers
-    rows[:, 3:6] = normals
-    rows[:, 6:9] = e1
-    rows[:, 9:12] = e2
-    rows[:, 12] = areas
-    rows_t = torch.from_numpy(rows).to(device)
-    order_t = torch.from_numpy(np.ascontiguousarray(order, np.int64)).to(
-        device)
-    soa = rows_t.index_select(0, order_t).t().contiguous()
+
+    def up(a, cols):
+        t = torch.from_numpy(np.ascontiguousarray(a, np.float64)).to(device)
+        return t.reshape(n, cols)
+    rows_t = torch.cat([up(centers, 3), up(normals, 3), up(e1, 3), up(e2, 3),
+                        up(areas, 1)], 1)
+    order_t = (order if isinstance(order, torch.Tensor) else
+               torch.from_numpy(np.ascontiguousarray(order, np.int64)).to(
+                   device))
+    soa = rows_t.to(torch.float32).index_select(0, order_t).t().contiguous()
     extras = {}
     if gamma is not None:
-        extras["gamma_f32"] = _dev(np.asarray(gamma, np.float32)[order],
-                                   np.float32, device)
+        extras["gamma_f32"] = permuted(gamma, np.float32, order_t, device)
     if sigma is not None:
-        extras["sigma"] = _dev(np.asarray(sigma, np.float32)[order],
-                               np.float32, device)
+        extras["sigma"] = permuted(sigma, np.float32, order_t, device)
     if corr is not None:
-        extras["corr"] = _dev(np.asarray(corr, np.float32)[order],
-                              np.float32, device)
+        extras["corr"] = permuted(corr, np.float32, order_t, device)
     if phasors is not None:
-        ph = np.asarray(phasors, np.complex64)[order]
-        extras["phasor"] = _dev(ph.view(np.float32), np.float32, device)
+        ph = np.ascontiguousarray(phasors, np.complex64).view(
+            np.float32).reshape(n, 2)
+        extras["phasor"] = permuted(ph, np.float32, order_t,
+                                    device).reshape(-1)
     return DeviceFacets(soa, extras, n)
 
 
@@ -183,7 +206,7 @@ class CoherentPlan:
         res = _field_to_host(field, out_dtype)
         if self.split:
             res = res.reshape(self.T, self.n_samples, 2)
-        return res, dropped.cpu().numpy().astype(np.float32)
+        return res, to_host(dropped.to(torch.float32))
 
 
 def coherent_run_count(plan):
@@ -203,7 +226,7 @@ def prepare_coherent(positions, u_ct, centers, normals, areas, e1, e2, *, k,
     n = np.asarray(centers).shape[0]
     plan = cull_plan(pos, centers, t0=t0, dt=dt, n_samples=n_samples, c=c,
                      block_size=block_size, target_pairs=1 << 19,
-                     window_cull=window_cull)
+                     window_cull=window_cull, device=device)
     gamma_arr = np.asarray(gamma, np.float32)
     gamma_facet = gamma_arr.ndim > 0
     if gamma_facet and gamma_arr.shape != (n,):

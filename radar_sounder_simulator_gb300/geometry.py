@@ -11,6 +11,7 @@ test-suite.
 from typing import NamedTuple
 
 import numpy as np
+import torch
 
 
 def window_reach_m(t0, dt, n_samples, c):
@@ -26,7 +27,9 @@ def auto_block_size(n_traces, target_pairs, lo=512, hi=16384):
 
 
 class CullPlan(NamedTuple):
-    order: np.ndarray      # (N,) facet permutation (stable along-track sort)
+    order: object          # (N,) facet permutation (stable along-track sort):
+    #                        int64 ndarray, or an int64 device tensor when
+    #                        the plan was made for a CUDA device
     block_size: int
     n_blocks: int
     off: np.ndarray        # (T,) int32 first block of each trace window
@@ -34,8 +37,15 @@ class CullPlan(NamedTuple):
 
 
 def cull_plan(positions, centers, *, t0, dt, n_samples, c, block_size,
-              target_pairs, window_cull=True):
-    """Order + windows as coherent.py:284-296 / multilayer.py:684-697."""
+              target_pairs, window_cull=True, device=None):
+    """Order + windows as coherent.py:284-296 / multilayer.py:684-697.
+
+    With a CUDA ``device`` the sort and the window searches run there: the
+    projections are computed on the host exactly as the reference computes
+    them, uploaded, stably sorted (equal keys keep their index order, -0.0
+    counts as +0.0, as in NumPy's comparison) and searched on the device;
+    the permutation stays there as an int64 tensor and only the per-trace
+    window offsets come back."""
     pos = np.asarray(positions, np.float64)
     cen = np.asarray(centers, np.float64)
     n = len(cen)
@@ -45,6 +55,9 @@ def cull_plan(positions, centers, *, t0, dt, n_samples, c, block_size,
     nrm = np.linalg.norm(d)
     axis = d / nrm if nrm > 0 else np.array([1.0, 0.0])
     s_f = cen[:, :2] @ axis
+    if device is not None and torch.device(device).type == "cuda":
+        return _cull_plan_device(s_f + 0.0, pos[:, :2] @ axis, bs, n_blocks,
+                                 t0, dt, n_samples, c, window_cull, device)
     order = np.argsort(s_f, kind="stable")
     s_sorted = s_f[order]
     s_t = pos[:, :2] @ axis
@@ -56,6 +69,26 @@ def cull_plan(positions, centers, *, t0, dt, n_samples, c, block_size,
     hi = np.searchsorted(s_sorted, s_t + reach, "right")
     b_lo = lo // bs
     b_hi = np.minimum(-(-hi // bs), n_blocks)
+    n_win = int(max(1, int((b_hi - b_lo).max())))
+    off = np.minimum(b_lo, n_blocks - n_win).astype(np.int32)
+    return CullPlan(order, bs, n_blocks, off, n_win)
+
+
+def _cull_plan_device(s_f, s_t, bs, n_blocks, t0, dt, n_samples, c,
+                      window_cull, device):
+    keys = torch.from_numpy(s_f).to(device)
+    s_sorted, order = torch.sort(keys, stable=True)
+    if not window_cull:
+        return CullPlan(order, bs, n_blocks, np.zeros(len(s_t), np.int32),
+                        int(n_blocks))
+    reach = window_reach_m(t0, dt, n_samples, c)
+    lo_v = torch.from_numpy(s_t - reach).to(device)
+    hi_v = torch.from_numpy(s_t + reach).to(device)
+    lo = torch.searchsorted(s_sorted, lo_v, right=False)
+    hi = torch.searchsorted(s_sorted, hi_v, right=True)
+    lh = torch.stack([lo, hi]).cpu().numpy()
+    b_lo = lh[0] // bs
+    b_hi = np.minimum(-(-lh[1] // bs), n_blocks)
     n_win = int(max(1, int((b_hi - b_lo).max())))
     off = np.minimum(b_lo, n_blocks - n_win).astype(np.int32)
     return CullPlan(order, bs, n_blocks, off, n_win)

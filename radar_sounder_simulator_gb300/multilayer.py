@@ -17,45 +17,73 @@ import numpy as np
 import torch
 
 from . import _lib
-from .coherent import (_dev, _field_to_host, pattern_struct, rough_struct,
-                       stage_facets)
+from .coherent import (_dev, _field_to_host, pattern_struct, permuted,
+                       rough_struct, stage_facets, to_host)
 from .geometry import cull_plan
 
 
-def _affine_fit(x, y, rc):
+def _affine_fit(cen, rc):
     """Least-squares (x, y, 1) -> (row, col) fit, the problem
     multilayer.py:277-278 hands to lstsq, solved through the 2x2 normal
-    equations of the centred coordinates (well conditioned, O(N), equal to
-    the SVD solution to float64 rounding). Returns coef (3, 2): rows x, y, 1."""
-    mx, my = x.mean(), y.mean()
-    xc, yc = x - mx, y - my
-    sxx, sxy, syy = xc @ xc, xc @ yc, yc @ yc
-    det = sxx * syy - sxy * sxy
-    if not det > 1e-12 * max(sxx * syy, 1e-300):
-        a = np.column_stack([x, y, np.ones(len(x))])
+    equations of the centred coordinates (equal to the SVD solution to
+    float64 rounding for a frame centred near the scene). The moments come
+    from two matrix products over the (N, 3) centres, so the fit costs about
+    one pass over the data. ``rc`` (N, 2). Returns coef (3, 2): rows x, y,
+    1."""
+    n = len(cen)
+    G = cen.T @ cen                       # raw second moments
+    m = (np.ones(n) @ cen) / n            # means
+    S = G[:2, :2] - n * np.outer(m[:2], m[:2])
+    det = S[0, 0] * S[1, 1] - S[0, 1] * S[1, 0]
+    if not det > 1e-12 * max(S[0, 0] * S[1, 1], 1e-300):
+        a = np.column_stack([cen[:, :2], np.ones(n)])
         return np.linalg.lstsq(a, rc, rcond=None)[0]
-    mr = rc.mean(0)
-    rcc = rc - mr
-    bx, by = xc @ rcc, yc @ rcc
-    cx = (syy * bx - sxy * by) / det
-    cy = (sxx * by - sxy * bx) / det
-    return np.vstack([cx, cy, mr - cx * mx - cy * my])
+    mr = (np.ones(n) @ rc) / n
+    B = (cen.T @ rc)[:2] - n * np.outer(m[:2], mr)
+    cx = (S[1, 1] * B[0] - S[0, 1] * B[1]) / det
+    cy = (S[0, 0] * B[1] - S[0, 1] * B[0]) / det
+    return np.vstack([cx, cy, mr - cx * m[0] - cy * m[1]])
 
 
-def grid_consts(f):
+def grid_consts_device(f, device):
     """Lookup table (ny, nx, 6) float32 [centre, normal], affine (x, y, 1) ->
     (row, col) least-squares fit, area-weighted mean point and unit normal
-    (multilayer.py:269-283)."""
+    (multilayer.py:269-283). The per-facet work runs on the device: one
+    float64 upload of centres, normals, areas and cells, the float32 table
+    and the moments of the fit and the mean plane formed there, 27 numbers
+    back. Returns (table tensor on ``device``, coef (3, 2), mean point, unit
+    mean normal)."""
     ny, nx = f.grid_shape
-    tab = np.concatenate([
-        np.asarray(f.centers).reshape(ny, nx, 3).astype(np.float32),
-        np.asarray(f.normals).reshape(ny, nx, 3).astype(np.float32)], -1)
-    cen = np.asarray(f.centers, np.float64)
-    coef = _affine_fit(cen[:, 0], cen[:, 1], np.asarray(f.cell, np.float64))
-    areas = np.asarray(f.areas, np.float64)
-    w = (areas / areas.sum())[:, None]
-    mp = (cen * w).sum(0)
-    mn = (np.asarray(f.normals, np.float64) * w).sum(0)
+    cen = torch.from_numpy(np.ascontiguousarray(f.centers, np.float64)).to(
+        device)
+    nrm = torch.from_numpy(np.ascontiguousarray(f.normals, np.float64)).to(
+        device)
+    area = torch.from_numpy(np.ascontiguousarray(f.areas, np.float64)).to(
+        device)
+    rc = torch.from_numpy(np.ascontiguousarray(f.cell)).to(device).to(
+        torch.float64)
+    tab = torch.cat([cen, nrm], 1).to(torch.float32).reshape(ny, nx, 6)
+    n = cen.shape[0]
+    small = torch.cat([(cen.T @ cen).reshape(-1), cen.sum(0), rc.sum(0),
+                       (cen.T @ rc).reshape(-1), area.sum().reshape(1),
+                       area @ cen, area @ nrm]).cpu().numpy()
+    G = small[0:9].reshape(3, 3)
+    m = small[9:12] / n
+    mr = small[12:14] / n
+    CR = small[14:20].reshape(3, 2)
+    sa = small[20]
+    mp = small[21:24] / sa
+    mn = small[24:27]
+    S = G[:2, :2] - n * np.outer(m[:2], m[:2])
+    det = S[0, 0] * S[1, 1] - S[0, 1] * S[1, 0]
+    if not det > 1e-12 * max(S[0, 0] * S[1, 1], 1e-300):
+        coef = _affine_fit(np.asarray(f.centers, np.float64),
+                           np.asarray(f.cell, np.float64))
+    else:
+        B = CR[:2] - n * np.outer(m[:2], mr)
+        cx = (S[1, 1] * B[0] - S[0, 1] * B[1]) / det
+        cy = (S[0, 0] * B[1] - S[0, 1] * B[0]) / det
+        coef = np.vstack([cx, cy, mr - cx * m[0] - cy * m[1]])
     return tab, coef, mp, mn / np.linalg.norm(mn)
 
 
@@ -123,10 +151,10 @@ class RefractedPlan:
         else:
             res = field[..., 0].to(torch.float32 if (out_dtype or np.float32)
                                    == np.float32 else torch.float64)
-            res = res.cpu().numpy().astype(out_dtype or np.float32)
+            res = to_host(res).astype(out_dtype or np.float32, copy=False)
         if self.split:
             res = res.reshape(self.T, self.n_samples, 2)
-        return res, dropped.cpu().numpy().astype(np.float32)
+        return res, to_host(dropped.to(torch.float32))
 
 
 def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
@@ -170,7 +198,7 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
         att = np.concatenate([np.full(k_pad, att[0]), att])
         if sig_c is not None:
             sig_c = np.concatenate([np.zeros(k_pad), sig_c])
-    ifaces += [grid_consts(f) for f in crossed]
+    ifaces += [grid_consts_device(f, device) for f in crossed]
     ni = len(ifaces)
     if not 1 <= ni <= 8:
         raise ValueError(f"{ni} crossed interfaces; the kernel takes 1..8")
@@ -178,7 +206,8 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
         raise ValueError("eps_leg/att_leg need len(crossed) + 1 entries")
     arr = (_lib.Interface * ni)()
     for j, (tab, coef, mp, mn) in enumerate(ifaces):
-        t = _dev(tab, np.float32, device)
+        t = (tab if isinstance(tab, torch.Tensor)
+             else _dev(tab, np.float32, device))
         keep.append(t)
         arr[j].table = t.data_ptr()
         arr[j].ny, arr[j].nx = tab.shape[0], tab.shape[1]
@@ -194,7 +223,7 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
     bs_req = block_size or (4096 if joint else None)
     plan = cull_plan(pos, centers, t0=t0, dt=dt, n_samples=n_samples, c=c,
                      block_size=bs_req, target_pairs=1 << 18,
-                     window_cull=window_cull)
+                     window_cull=window_cull, device=device)
     rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
     fac = stage_facets(centers, target.normals, target.areas, target.e1,
                        target.e2, plan.order, device, sigma=s_arr,
@@ -207,17 +236,18 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
         d_amp = np.asarray(d_amp, np.float64)
         if d_amp.shape != (n,):
             raise ValueError(f"diffuse amp shape {d_amp.shape} != ({n},)")
-        fac.extras["diffuse_amp"] = _dev(d_amp[plan.order], np.float64,
-                                         device)
-        fac.extras["diffuse_phasor"] = _dev(
-            np.asarray(d_ph, np.complex64)[plan.order].view(np.float32),
-            np.float32, device)
+        fac.extras["diffuse_amp"] = permuted(d_amp, np.float64, plan.order,
+                                             device)
+        fac.extras["diffuse_phasor"] = permuted(
+            np.ascontiguousarray(d_ph, np.complex64).view(
+                np.float32).reshape(n, 2), np.float32, plan.order,
+            device).reshape(-1)
     if gamma_facet:
         if gamma_arr.shape != (n,):
             raise ValueError(f"per-facet gamma shape {gamma_arr.shape} != "
                              f"({n},)")
-        fac.extras["gamma_f64"] = _dev(gamma_arr[plan.order], np.float64,
-                                       device)
+        fac.extras["gamma_f64"] = permuted(gamma_arr, np.float64,
+                                           plan.order, device)
     pst, pv_t, pv_len, pkeep = pattern_struct(pattern, T, device)
     pos_t = _dev(pos, np.float64, device)
     uct_t = _dev(np.asarray(u_ct, np.float64).reshape(T, 3), np.float64,
