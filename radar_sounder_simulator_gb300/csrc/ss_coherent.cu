@@ -74,6 +74,12 @@ __device__ __forceinline__ void coherent_fp64_cta(const CoArgs &a, int chunk,
 
   const double k = a.k;
   const double amp_pref = k / kTwoPi;
+  // traces rotated across lanes and dropped power kept per thread, as in
+  // the split form (ss_coherent_split.cu)
+  const int rot = (tid & 31) % max(nt, 1);
+  double dropl[SS_MAX_TB];
+#pragma unroll
+  for (int j = 0; j < SS_MAX_TB; ++j) dropl[j] = 0.0;
   for (int i = s_rng[0] + tid; i < s_rng[1]; i += blockDim.x) {
     const double cx = a.F.cx[i], cy = a.F.cy[i], cz = a.F.cz[i];
     const double nx = a.F.nx[i], ny = a.F.ny[i], nz = a.F.nz[i];
@@ -81,7 +87,8 @@ __device__ __forceinline__ void coherent_fp64_cta(const CoArgs &a, int chunk,
     const double e2x = a.F.e2x[i], e2y = a.F.e2y[i], e2z = a.F.e2z[i];
     const double area = a.F.area[i];
     const double gam = a.F.gamma_f32 ? (double)a.F.gamma_f32[i] : a.gamma;
-    for (int tt = 0; tt < nt; ++tt) {
+    for (int st = 0; st < nt; ++st) {
+      const int tt = rot + st < nt ? rot + st : rot + st - nt;
       if (i < s_lo[tt] || i >= s_hi[tt]) continue;
       // range chain in round-to-nearest (bins bit-identical to NumPy)
       const double dx = __dsub_rn(s_p[tt][0], cx);
@@ -153,17 +160,19 @@ __device__ __forceinline__ void coherent_fp64_cta(const CoArgs &a, int chunk,
             atomicAdd(&h[(int)bq].x, pr);
             atomicAdd(&h[(int)bq].y, pim);
           } else {
-            atomicAdd(&s_drop[tt], pr * pr + pim * pim);
+            dropl[tt] += pr * pr + pim * pim;
           }
         }
       } else if (fb >= 0.0 && fb < (double)a.n_samples) {
         atomicAdd(&h[(int)fb].x, re);
         atomicAdd(&h[(int)fb].y, im);
       } else {
-        atomicAdd(&s_drop[tt], re * re + im * im);
+        dropl[tt] += re * re + im * im;
       }
     }
   }
+  for (int tt = 0; tt < nt; ++tt)
+    if (dropl[tt] != 0.0) atomicAdd(&s_drop[tt], dropl[tt]);
   __syncthreads();
   double2 *part = reinterpret_cast<double2 *>(a.part);
   for (int tt = 0; tt < nt; ++tt) {

@@ -109,6 +109,14 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   __syncthreads();
 
   const float nsf = (float)a.n_samples;
+  // lane l meets the block's traces starting at trace l mod nt, so the 32
+  // neighbouring facets of a warp -- often in one bin -- spread their
+  // histogram atomics over the block's traces; dropped power collects per
+  // thread and trace and reaches shared memory once per trace at the end
+  const int rot = (tid & 31) % max(nt, 1);
+  float dropl[SS_MAX_TB];
+#pragma unroll
+  for (int j = 0; j < SS_MAX_TB; ++j) dropl[j] = 0.0f;
   for (int i = s_rng[0] + tid; i < s_rng[1]; i += blockDim.x) {
     const float cx = a.F.cx[i], cy = a.F.cy[i], cz = a.F.cz[i];
     const float nx = a.F.nx[i], ny = a.F.ny[i], nz = a.F.nz[i];
@@ -125,7 +133,8 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       l1 = sqrtf(dot3f(e1x, e1y, e1z, e1x, e1y, e1z));
       l2 = sqrtf(dot3f(e2x, e2y, e2z, e2x, e2y, e2z));
     }
-    for (int tt = 0; tt < nt; ++tt) {
+    for (int st = 0; st < nt; ++st) {
+      const int tt = rot + st < nt ? rot + st : rot + st - nt;
       if (i < s_lo[tt] || i >= s_hi[tt]) continue;
       // --- d = p - c as double-float per component ---
       float dxh, dxl, dyh, dyl, dzh, dzl, e;
@@ -240,17 +249,19 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
             atomicAdd(&h[(int)bq].x, pr);
             atomicAdd(&h[(int)bq].y, pim);
           } else {
-            atomicAdd(&s_drop[tt], pr * pr + pim * pim);
+            dropl[tt] += pr * pr + pim * pim;
           }
         }
       } else if (fb >= 0.0f && fb < nsf) {
         atomicAdd(&h[(int)fb].x, re);
         atomicAdd(&h[(int)fb].y, im);
       } else {
-        atomicAdd(&s_drop[tt], re * re + im * im);
+        dropl[tt] += re * re + im * im;
       }
     }
   }
+  for (int tt = 0; tt < nt; ++tt)
+    if (dropl[tt] != 0.0f) atomicAdd(&s_drop[tt], dropl[tt]);
   __syncthreads();
   float2 *part = reinterpret_cast<float2 *>(a.part);
   for (int tt = 0; tt < nt; ++tt) {
