@@ -49,7 +49,8 @@ def parse():
                          "an ncu capture of the same workload (reported in "
                          "the roofline object; default: the one-pass capture "
                          "of the bed launch at the default size)")
-    ap.add_argument("--rows", default="cfg1,modef,cfg3,cfg4,cfg5,incoh,focus",
+    ap.add_argument("--rows",
+                    default="cfg1,modef,cfg3,cfg4,cfg5,incoh,focus,scene",
                     help="secondary workloads measured after the headline "
                          "(comma list, or 'none')")
     ap.add_argument("--batch-instances", type=int, default=96)
@@ -813,6 +814,60 @@ def row_focus(device, flush, peaks):
             "error_vs_fp64": _errors(res["split"], res["fp64"])}
 
 
+def row_scene(device, flush):
+    """Scene assembly: a 513 x 513 EPSG:3413 DEM window (50 m posting) to
+    262,144 local-frame facets, their keyed speckle phasors and a 300 m
+    offset interface."""
+    import torch
+    from oracle import scene as osc
+    from radar_sounder_simulator_gb300 import scene as gsc
+    rng = np.random.default_rng(11)
+    cx, cy = osc.polar_stereo_forward(-40.0, 75.0, "EPSG:3413")
+    n, post = 513, 50.0
+    tr = (post, 0.0, cx - n * post / 2, 0.0, -post, cy + n * post / 2)
+    dem = 800.0 + np.cumsum(rng.normal(0, 1.0, (n, n)), axis=1)
+    frame = gsc.LocalFrame(75.0, -40.0, 0.0)
+
+    def dev_step():
+        f = gsc.build_facets(dem, tr, "EPSG:3413", frame, device=device,
+                             as_tensors=True)
+        gsc.speckle_phasors_tensor(f.phase_keys, (3, 1))
+        return f
+    ms = _events_ms(dev_step, 5, flush)
+    f = gsc.build_facets(dem, tr, "EPSG:3413", frame, device=device)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f = gsc.build_facets(dem, tr, "EPSG:3413", frame, device=device)
+    gsc.speckle_phasors_for_keys(f.phase_keys, (3, 1), device=device)
+    gsc.offset_facets(f, frame, -300.0, device=device)
+    e2e_ms = (time.perf_counter() - t0) * 1e3
+    nf = len(f.centers)
+    # CPU baseline: the float64 NumPy oracle (the reference's algorithm,
+    # projection restated), one core, the same window
+    ofr = osc.LocalFrame(75.0, -40.0, 0.0)
+
+    def to_ecef(E, N, h):
+        lo, la = osc.polar_stereo_inverse(E, N, "EPSG:3413")
+        return osc.geodetic_to_ecef(la, lo, h)
+    t0 = time.perf_counter()
+    ref = osc.build_facets(dem, tr, to_ecef, ofr.ecef_to_local)
+    osc.speckle_phasors_for_keys(ref["phase_keys"], (3, 1))
+    osc.offset_centers(ref["centers"], ofr, -300.0)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "dem_513sq_epsg3413_to_262144_facets",
+            "unit": "facets/s", "value": nf / (ms * 1e-3),
+            "ms_per_step": ms,
+            "e2e": {"value": nf / (e2e_ms * 1e-3), "ms": e2e_ms,
+                    "note": "host DEM in, NumPy facets, phasors and offset "
+                            "interface out"},
+            "cpu_baseline": {"value": nf / cpu_s, "unit": "facets/s",
+                             "cores": 1, "kind": "port",
+                             "sample": "the same window, float64 NumPy "
+                                       "oracle (facets, phasors, offset)"},
+            "note": "device-resident step: lattice upload, vertices, "
+                    "corner rule, keyed phasors"}
+
+
 def run_rows(args, device, peak32):
     import torch
     want = [] if args.rows == "none" else args.rows.split(",")
@@ -830,7 +885,8 @@ def run_rows(args, device, peak32):
                                     peaks),
            "cfg5": lambda: row_cfg5(device, flush),
            "incoh": lambda: row_incoh(device, flush, peaks),
-           "focus": lambda: row_focus(device, flush, peaks)}
+           "focus": lambda: row_focus(device, flush, peaks),
+           "scene": lambda: row_scene(device, flush)}
     for name in want:
         t0 = time.perf_counter()
         try:

@@ -317,6 +317,64 @@ int ss_focused_sar(const ss_focus_opts *opts, const void *field,
                    const ss_focus_output *out, void *scratch,
                    size_t scratch_bytes, void *stream);
 
+/* ---- scene assembly ---------------------------------------------------- */
+
+/* Projected CRS of a DEM window (the reference takes any CRS from pyproj;
+ * these are the ones its synthetic scenes and ice-sheet DEMs use). */
+#define SS_PROJ_IDENTITY 0     /* projected (E, N, h) already are ECEF      */
+#define SS_PROJ_POLAR_NORTH 1  /* EPSG:3413, WGS84 polar stereographic N    */
+#define SS_PROJ_POLAR_SOUTH 2  /* EPSG:3031, WGS84 polar stereographic S    */
+
+/* ENU frame (scene.py:24-82 LocalFrame): local = R (ecef - origin), R's
+ * rows the E, N, U unit vectors in ECEF, row-major. */
+typedef struct {
+  double origin[3];
+  double R[9];
+} ss_frame;
+
+/* A DEM window sampled on its facet lattice (scene.py:126-156). */
+typedef struct {
+  const double *dem;       /* (device) (ny, nx) heights above WGS84 (m)   */
+  int32_t ny, nx;
+  const double *rows;      /* (device) (n_rows,) fractional pixel rows    */
+  const double *cols;      /* (device) (n_cols,) fractional pixel columns */
+  int32_t n_rows, n_cols;
+  double transform[6];     /* pixel (x, y) -> (x a + y b + c, x d + y e + f),
+                              (a, b, c, d, e, f)                          */
+  int32_t projection;      /* SS_PROJ_*                                    */
+  ss_frame frame;
+} ss_dem_grid;
+
+/* Vertices (n_rows, n_cols, 3) float64 in the local frame: bilinear DEM
+ * sample at each lattice point (scene.py:104-112), pixel centre through the
+ * affine transform, projected -> geodetic -> ECEF (WGS84) -> local. */
+int ss_scene_vertices(const ss_dem_grid *grid, double *vertices,
+                      void *stream);
+
+/* Mean-plane facets of a vertex grid (scene.py:158-176). Any output may be
+ * NULL. centers/normals/e1/e2 (N, 3), areas (N,), cell and phase_keys
+ * (N, 2) int64 (phase_keys from row_keys[i], col_keys[j]); N = (H-1)(W-1),
+ * facet (i, j) at i (W-1) + j. */
+typedef struct {
+  double *centers, *normals, *areas, *e1, *e2;
+  int64_t *cell, *phase_keys;
+} ss_facet_out;
+
+int ss_facets_from_vertices(const double *vertices, int32_t H, int32_t W,
+                            const int64_t *row_keys, const int64_t *col_keys,
+                            const ss_facet_out *out, void *stream);
+
+/* Stateless Gaussian speckle phasors of (n, 2) int64 parent-grid keys
+ * (roughness.py:207-233); base = the seed's SeedSequence state word.
+ * out: (n,) complex64 interleaved (device). */
+int ss_speckle_phasors_keyed(const int64_t *keys, int64_t n, uint64_t base,
+                             float *out, void *stream);
+
+/* Facet centres moved `offset` metres along local ellipsoidal up
+ * (layered.py:38-53 offset_facets; normals, areas and edges unchanged). */
+int ss_offset_centers(const double *centers, int64_t n, const ss_frame *frame,
+                      double offset, double *out, void *stream);
+
 /* Batched surface coherent sums (no counterpart in the reference, which
  * calls coherent_cluttergram once per scene): one job per call of
  * ss_coherent_fwd, all jobs of a batch with the same precision and

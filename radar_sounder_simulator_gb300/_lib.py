@@ -17,6 +17,7 @@ PATTERN = {"isotropic": 0, "dipole": 1, "array": 2, "array_tapered": 3,
            "finite_dipole": 4, "tabulated": 5}
 ROUGH_NONE, ROUGH_GAUSS_FULL, ROUGH_GAUSS_AREA, ROUGH_EXP_AREA = range(4)
 WIN_HANN, WIN_RECT = range(2)
+PROJ = {None: 0, "EPSG:3413": 1, "EPSG:3031": 2}
 
 _f = C.POINTER(C.c_float)
 _d = C.POINTER(C.c_double)
@@ -139,6 +140,23 @@ class FocusOutput(C.Structure):
                 ("power", C.c_void_p)]
 
 
+class Frame(C.Structure):
+    _fields_ = [("origin", C.c_double * 3), ("R", C.c_double * 9)]
+
+
+class DemGrid(C.Structure):
+    _fields_ = [("dem", C.c_void_p), ("ny", C.c_int32), ("nx", C.c_int32),
+                ("rows", C.c_void_p), ("cols", C.c_void_p),
+                ("n_rows", C.c_int32), ("n_cols", C.c_int32),
+                ("transform", C.c_double * 6), ("projection", C.c_int32),
+                ("frame", Frame)]
+
+
+class FacetOut(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in (
+        "centers", "normals", "areas", "e1", "e2", "cell", "phase_keys")]
+
+
 class BatchInfo(C.Structure):
     _fields_ = [("n_jobs", C.c_int32), ("precision", C.c_int32),
                 ("rough_kind", C.c_int32), ("threads", C.c_int32),
@@ -209,6 +227,16 @@ SIGNATURES = {
                                  C.c_void_p, C.c_void_p,
                                  C.POINTER(FocusOutput), C.c_void_p,
                                  C.c_size_t, C.c_void_p]),
+    "ss_scene_vertices": (C.c_int, [C.POINTER(DemGrid), C.c_void_p,
+                                    C.c_void_p]),
+    "ss_facets_from_vertices": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32,
+                                          C.c_void_p, C.c_void_p,
+                                          C.POINTER(FacetOut), C.c_void_p]),
+    "ss_speckle_phasors_keyed": (C.c_int, [C.c_void_p, C.c_int64,
+                                           C.c_uint64, C.c_void_p,
+                                           C.c_void_p]),
+    "ss_offset_centers": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Frame),
+                                    C.c_double, C.c_void_p, C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
     "ss_fp64_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,

@@ -413,6 +413,83 @@ def make_focus(ns):
     return out
 
 
+class _AffineLike:
+    """Stand-in for affine.Affine (absent here): the attributes and the
+    point mapping build_facets uses, (x a + y b + c, x d + y e + f)."""
+
+    def __init__(self, a, b, c, d, e, f):
+        self.a, self.b, self.c, self.d, self.e, self.f = a, b, c, d, e, f
+
+    def __mul__(self, xy):
+        x, y = xy
+        return (x * self.a + y * self.b + self.c,
+                x * self.d + y * self.e + self.f)
+
+
+class _ShiftFrame:
+    """LocalFrame stand-in: ECEF -> local is a shift (identity rotation)."""
+
+    def __init__(self, origin):
+        self.origin = np.asarray(origin, np.float64)
+
+    def ecef_to_local(self, xyz):
+        return np.atleast_2d(xyz) - self.origin
+
+
+def _pyproj_identity():
+    """pyproj stand-in whose transforms are the identity, so build_facets'
+    DEM -> projected -> 'ECEF' chain reduces to its own arithmetic."""
+    import types
+    mod = types.ModuleType("pyproj")
+
+    class Transformer:
+        @staticmethod
+        def from_crs(*_a, **_k):
+            return Transformer()
+
+        def transform(self, x, y, z=None):
+            return (x, y) if z is None else (x, y, z)
+    mod.Transformer = Transformer
+    mod.Proj = None
+    sys.modules["pyproj"] = mod
+
+
+def make_scene(ns):
+    """Keyed speckle phasors (roughness.py:207-233) and build_facets
+    (scene.py:126-176) through an identity pyproj stand-in and a shift
+    frame: lattice, bilinear resampling, affine mapping and corner rule."""
+    out = {}
+    r, c = np.meshgrid(np.arange(-40, 260, 3), np.arange(700, 980, 7),
+                       indexing="ij")
+    keys = np.column_stack([r.ravel(), c.ravel()]).astype(np.int64)
+    keys = np.concatenate([keys, [[0, 0], [2**40, -5], [-2**45, 2**33]]])
+    out["keys"] = keys
+    for name, seed in (("s31", (3, 1)), ("s7", 7), ("s11_1002", (11, 1002))):
+        out[f"phasors_{name}"] = ns.roughness.speckle_phasors_for_keys(
+            keys, seed)
+    _pyproj_identity()
+    scene = refload.importlib.import_module("soundersim.scene")
+    rng = np.random.default_rng(51)
+    dem = (800.0 + np.cumsum(rng.normal(0, 2.0, (22, 20)), axis=1)
+           + 3.0 * rng.standard_normal((22, 20)))
+    tr = (25.0, 0.0, 1000.0, 0.0, -25.0, 5000.0)
+    origin = np.array([1400.0, 4500.0, 790.0])
+    out.update(dem=dem, transform=np.array(tr), origin=origin)
+    for name, sp, go in (("native", None, (0, 0)), ("stride", 50.0, (0, 0)),
+                         ("fine", 10.0, (0, 0)),
+                         ("crop", 50.0, (3, 5))):
+        f = scene.build_facets(dem, _AffineLike(*tr), "EPSG:3413",
+                               _ShiftFrame(origin), spacing=sp,
+                               grid_origin=go)
+        out[f"bf_{name}_spacing"] = np.nan if sp is None else sp
+        out[f"bf_{name}_origin"] = np.array(go)
+        for k in ("centers", "normals", "areas", "e1", "e2", "cell",
+                  "phase_keys"):
+            out[f"bf_{name}_{k}"] = getattr(f, k)
+        out[f"bf_{name}_grid"] = np.array(f.grid_shape)
+    return out
+
+
 def main():
     only = None
     args = [a for a in sys.argv[1:]]
@@ -429,7 +506,8 @@ def main():
                      ("refracted", make_refracted),
                      ("waveform", make_waveform),
                      ("incoherent", make_incoherent),
-                     ("focus", make_focus)):
+                     ("focus", make_focus),
+                     ("scene", make_scene)):
         if only is not None and name not in only:
             continue
         data = fn(ns)

@@ -54,7 +54,9 @@ def test_struct_layouts_match_header(tmp_path):
                "ss_incoherent_opts": _lib.IncoherentOpts,
                "ss_incoherent_output": _lib.IncoherentOutput,
                "ss_focus_opts": _lib.FocusOpts,
-               "ss_focus_output": _lib.FocusOutput}
+               "ss_focus_output": _lib.FocusOutput,
+               "ss_frame": _lib.Frame, "ss_dem_grid": _lib.DemGrid,
+               "ss_facet_out": _lib.FacetOut}
     lines = ["#include <stdio.h>", "#include <stddef.h>",
              '#include "soundersim_gb300.h"', "int main(void) {"]
     for cname, py in structs.items():
