@@ -117,12 +117,16 @@ __device__ __forceinline__ float gain32(int kind, int n, int pa_len,
       float th = acosf(ct);
       if (th <= pa[0]) return pb[0];
       if (th >= pa[n - 1]) return pb[n - 1];
-      int lo = 0, hi = n - 1;
-      while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (pa[mid] <= th) lo = mid; else hi = mid;
-      }
-      float slope = (pb[hi] - pb[lo]) / (pa[hi] - pa[lo]);
+      // segment with pa[lo] <= th < pa[lo + 1]: guessed from the mean
+      // spacing (exact for the usual evenly sampled tables), then walked;
+      // the same segment a binary search finds, for any ascending table
+      const float span = pa[n - 1] - pa[0];
+      int lo = (int)((th - pa[0]) * __fdividef((float)(n - 1), span));
+      lo = min(max(lo, 0), n - 2);
+      while (lo < n - 2 && pa[lo + 1] <= th) ++lo;
+      while (lo > 0 && pa[lo] > th) --lo;
+      const int hi = lo + 1;
+      float slope = __fdividef(pb[hi] - pb[lo], pa[hi] - pa[lo]);
       return __fmaf_rn(slope, th - pa[lo], pb[lo]);
     }
     default:
