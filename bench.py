@@ -50,7 +50,8 @@ def parse():
                          "the roofline object; default: the one-pass capture "
                          "of the bed launch at the default size)")
     ap.add_argument("--rows",
-                    default="cfg1,modef,cfg3,cfg4,cfg5,incoh,focus,scene",
+                    default="cfg1,modef,cfg3,cfg4,cfg5,incoh,focus,scene,"
+                            "output",
                     help="secondary workloads measured after the headline "
                          "(comma list, or 'none')")
     ap.add_argument("--batch-instances", type=int, default=96)
@@ -868,6 +869,51 @@ def row_scene(device, flush):
                     "corner rule, keyed phasors"}
 
 
+def row_output(device, flush):
+    """Per-trace output products (nadir and first return over every facet)
+    of the multilayer scene's surface under its 1024-trace line."""
+    import torch
+    from radar_sounder_simulator_gb300 import _lib, scenes
+    import ctypes as C_
+    cfg = scenes.config2()
+    f = cfg.layers[0]
+    cen = torch.as_tensor(np.ascontiguousarray(f.centers), device=device)
+    pos = torch.as_tensor(np.ascontiguousarray(cfg.pos), device=device)
+    T, N = len(cfg.pos), len(f.centers)
+    L = _lib.lib()
+    nb = L.ss_trace_products_scratch_bytes(T, N)
+    scratch = torch.empty(nb, dtype=torch.uint8, device=device)
+    res = [torch.empty(T, dtype=torch.int64, device=device),
+           torch.empty(T, dtype=torch.float64, device=device),
+           torch.empty(T, dtype=torch.int64, device=device),
+           torch.empty(T, dtype=torch.float64, device=device)]
+    o = _lib.TraceProductsOut(*[r.data_ptr() for r in res])
+    opts = _lib.TraceProductsOpts(cfg.t0, cfg.dt, cfg.c, cfg.n_samples)
+    stream = C_.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+    def run():
+        _lib.check(L.ss_trace_products(
+            C_.byref(opts), C_.c_void_p(cen.data_ptr()), N,
+            C_.c_void_p(pos.data_ptr()), T, C_.byref(o),
+            C_.c_void_p(scratch.data_ptr()), nb, stream),
+            "ss_trace_products")
+    ms = _events_ms(run, 5, flush)
+    from oracle import output as oout
+    t0 = time.perf_counter()
+    oout.trace_products(f.centers, cfg.pos[:8], cfg.t0, cfg.dt,
+                        cfg.n_samples, cfg.c)
+    cpu_s = time.perf_counter() - t0
+    return {"workload": "trace_products_262144_facets_1024tr",
+            "unit": "pairs/s", "value": T * N / (ms * 1e-3),
+            "ms_per_step": ms,
+            "cpu_baseline": {"value": 8 * N / cpu_s, "unit": "pairs/s",
+                             "cores": 1, "kind": "port",
+                             "sample": "8 traces x 262144 facets, float64 "
+                                       "NumPy oracle"},
+            "note": "nadir facet and first in-window arrival per trace, "
+                    "float32 screen + float64 decisions"}
+
+
 def run_rows(args, device, peak32):
     import torch
     want = [] if args.rows == "none" else args.rows.split(",")
@@ -886,7 +932,8 @@ def run_rows(args, device, peak32):
            "cfg5": lambda: row_cfg5(device, flush),
            "incoh": lambda: row_incoh(device, flush, peaks),
            "focus": lambda: row_focus(device, flush, peaks),
-           "scene": lambda: row_scene(device, flush)}
+           "scene": lambda: row_scene(device, flush),
+           "output": lambda: row_output(device, flush)}
     for name in want:
         t0 = time.perf_counter()
         try:

@@ -375,6 +375,38 @@ int ss_speckle_phasors_keyed(const int64_t *keys, int64_t n, uint64_t base,
 int ss_offset_centers(const double *centers, int64_t n, const ss_frame *frame,
                       double offset, double *out, void *stream);
 
+/* ---- per-trace output products ---------------------------------------- */
+
+/* output.py:47-82 build_dataset window (twtt axis t0 + k dt, k < n_samples)
+ * and wave speed. */
+typedef struct {
+  double t0, dt, c;
+  int32_t n_samples;
+} ss_trace_products_opts;
+
+/* Any output may be NULL. nadir: the horizontally nearest facet centre
+ * (first index on ties) and 2 (z_platform - z_facet) / c; first return:
+ * the facet with the earliest float64 twtt 2r/c inside [t0, t0 +
+ * n_samples dt) (first index on ties), or index 0 and +inf if none. */
+typedef struct {
+  int64_t *nadir_index;
+  double *nadir_twtt;
+  int64_t *first_index;
+  double *first_twtt;
+} ss_trace_products_out;
+
+size_t ss_trace_products_scratch_bytes(int32_t n_traces, int32_t n_facets);
+
+/* Every facet for every trace: centers (device) (N, 3) float64, positions
+ * (device) (T, 3) float64. Replaces the (T, N, 3) NumPy scans of
+ * output.py:64-82 (same results: float64 values in the reference's
+ * operation order, NumPy's first-index tie rule). */
+int ss_trace_products(const ss_trace_products_opts *opts,
+                      const double *centers, int32_t n_facets,
+                      const double *positions, int32_t n_traces,
+                      const ss_trace_products_out *out, void *scratch,
+                      size_t scratch_bytes, void *stream);
+
 /* Batched surface coherent sums (no counterpart in the reference, which
  * calls coherent_cluttergram once per scene): one job per call of
  * ss_coherent_fwd, all jobs of a batch with the same precision and

@@ -157,6 +157,16 @@ class FacetOut(C.Structure):
         "centers", "normals", "areas", "e1", "e2", "cell", "phase_keys")]
 
 
+class TraceProductsOpts(C.Structure):
+    _fields_ = [("t0", C.c_double), ("dt", C.c_double), ("c", C.c_double),
+                ("n_samples", C.c_int32)]
+
+
+class TraceProductsOut(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in (
+        "nadir_index", "nadir_twtt", "first_index", "first_twtt")]
+
+
 class BatchInfo(C.Structure):
     _fields_ = [("n_jobs", C.c_int32), ("precision", C.c_int32),
                 ("rough_kind", C.c_int32), ("threads", C.c_int32),
@@ -237,6 +247,11 @@ SIGNATURES = {
                                            C.c_void_p]),
     "ss_offset_centers": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(Frame),
                                     C.c_double, C.c_void_p, C.c_void_p]),
+    "ss_trace_products_scratch_bytes": (C.c_size_t, [C.c_int32, C.c_int32]),
+    "ss_trace_products": (C.c_int, [C.POINTER(TraceProductsOpts), C.c_void_p,
+                                    C.c_int32, C.c_void_p, C.c_int32,
+                                    C.POINTER(TraceProductsOut), C.c_void_p,
+                                    C.c_size_t, C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
     "ss_fp64_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,

@@ -490,6 +490,44 @@ def make_scene(ns):
     return out
 
 
+def make_output(ns):
+    """output.build_dataset (output.py:47-146) through the xarray stand-in:
+    the per-trace products it computes over every facet -- nadir twtt from
+    the horizontally nearest facet, first in-window arrival -- with an
+    identity frame so first_return_lat/lon name the facet's x, y."""
+    import types
+    xrshim.install()
+    sys.modules["soundersim"].__version__ = "reference"
+    out_mod = refload.importlib.import_module("soundersim.output")
+    surf = grid_scene(ns.Facets, 40, 25.0, 0.0, 1.5, seed=61,
+                      slope=(0.02, -0.03))
+    pos, _ = track(12, 900.0, 30.0)
+    pos = np.vstack([pos, [[60000.0, 0.0, 900.0]]])   # nothing in window
+    T = len(pos)
+    r = np.linalg.norm(pos[:12, None, :] - surf.centers[None], axis=-1)
+    t0 = 2 * (r.min() + 3.0) / C
+    dt, n_s = 1.0 / 60e6, 64
+    radar = types.SimpleNamespace(
+        c=C, t0=t0, dt=dt, f0=60e6, wavelength=C / 60e6,
+        waveform=types.SimpleNamespace(kind="delta"))
+    cfg = types.SimpleNamespace(radar=radar, mode="incoherent",
+                                model_dump_json=lambda: "{}")
+    scene = types.SimpleNamespace(nav_llh=pos, name="golden", crs="local",
+                                  params={})
+    frame = types.SimpleNamespace(lat0=0.0, lon0=0.0, h0=0.0,
+                                  local_to_llh=lambda enu: np.asarray(enu))
+    ds = out_mod.build_dataset(
+        np.zeros((T, n_s), np.float32), np.zeros(T, np.float32),
+        scene=scene, frame=frame, facets=surf,
+        track=types.SimpleNamespace(positions=pos), sim_config=cfg)
+    out = facet_dict("surf", surf)
+    out.update(pos=pos, t0=t0, dt=dt, n_samples=n_s)
+    for k in ("nadir_twtt", "first_return_twtt", "first_return_lat",
+              "first_return_lon"):
+        out[k] = np.asarray(ds[k].values)
+    return out
+
+
 def main():
     only = None
     args = [a for a in sys.argv[1:]]
@@ -507,7 +545,8 @@ def main():
                      ("waveform", make_waveform),
                      ("incoherent", make_incoherent),
                      ("focus", make_focus),
-                     ("scene", make_scene)):
+                     ("scene", make_scene),
+                     ("output", make_output)):
         if only is not None and name not in only:
             continue
         data = fn(ns)

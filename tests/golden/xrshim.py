@@ -28,9 +28,9 @@ class Dataset:
         self._vars = {}
         self._coords = {}
         for k, v in (data_vars or {}).items():
-            self._vars[k] = _as_array(v)
+            self._vars[k] = _as_array(v, k)
         for k, v in (coords or {}).items():
-            self._coords[k] = _as_array(v)
+            self._coords[k] = _as_array(v, k)
         self.attrs = dict(attrs or {})
 
     @property
@@ -64,15 +64,17 @@ class Dataset:
             raise AttributeError(name) from None
 
     def __setitem__(self, name, value):
-        self._vars[name] = _as_array(value)
+        self._vars[name] = _as_array(value, name)
 
     def copy(self):
         return copy.deepcopy(self)
 
 
-def _as_array(v):
+def _as_array(v, name):
     if isinstance(v, DataArray):
         return v
+    if not isinstance(v, tuple):      # a bare array: the dimension coord
+        return DataArray((name,), v)
     dims, values, *rest = v
     if isinstance(dims, str):
         dims = (dims,)

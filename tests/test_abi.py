@@ -56,7 +56,9 @@ def test_struct_layouts_match_header(tmp_path):
                "ss_focus_opts": _lib.FocusOpts,
                "ss_focus_output": _lib.FocusOutput,
                "ss_frame": _lib.Frame, "ss_dem_grid": _lib.DemGrid,
-               "ss_facet_out": _lib.FacetOut}
+               "ss_facet_out": _lib.FacetOut,
+               "ss_trace_products_opts": _lib.TraceProductsOpts,
+               "ss_trace_products_out": _lib.TraceProductsOut}
     lines = ["#include <stdio.h>", "#include <stddef.h>",
              '#include "soundersim_gb300.h"', "int main(void) {"]
     for cname, py in structs.items():
