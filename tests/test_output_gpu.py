@@ -85,14 +85,14 @@ def test_window_edges_decided_in_float64():
     (inside the screen's uncertain bands) next to facets well inside: the
     first return is the earliest facet truly in the window."""
     rng = np.random.default_rng(6)
-    p = np.array([[0.0, 0.0, 2000.0]])
+    p = np.array([[0.0, 0.0, 1500.0]])
     t0, dt, n_s = 2 * 1990.0 / C, 1e-8, 40
     r_start, r_end = C * t0 / 2, C * (t0 + n_s * dt) / 2
     rs = np.concatenate([r_start + rng.uniform(-5e-3, 5e-3, 200),
                          r_end + rng.uniform(-5e-3, 5e-3, 200),
                          rng.uniform(r_start + 1.0, r_end - 1.0, 50)])
     az = rng.uniform(0, 2 * np.pi, len(rs))
-    h = np.sqrt(rs ** 2 - (2000.0 - 10.0) ** 2)
+    h = np.sqrt(rs ** 2 - (1500.0 - 10.0) ** 2)
     cen = np.column_stack([h * np.cos(az), h * np.sin(az),
                            np.full(len(rs), 10.0)])
     kw = dict(t0=t0, dt=dt, n_samples=n_s, c=C)
