@@ -564,7 +564,7 @@ def row_modef(device, flush, peaks):
             "error_vs_fp64": _errors(res["split"], res["fp64"])}
 
 
-def row_cfg3(device, flush):
+def row_cfg3(device, flush, peaks):
     """Rough surface and bed, four bands: per band the surface coherent sum
     and the refracted bed sum (per-facet sigma, l; exponential ACF with the
     area-only series and taper), each pulse-compressed."""
@@ -608,16 +608,47 @@ def row_cfg3(device, flush):
             compress_tensor(f1, pulse, m)
             compress_tensor(f2, pulse, m)
         ms = _events_ms(step, 2, flush)
-        pairs = (len(s.centers) + len(b.centers)) * len(cfg.pos)
-        bands[f"{f0 / 1e6:.0f}MHz"] = {"ms": ms, "n_terms": [nt_s, nt_b],
-                                       "n_samples": n_s,
-                                       "contribs_per_s": pairs / (ms * 1e-3)}
+        ms_k = _events_ms(lambda: (ps.run(), pb.run()), 2, flush)
+        T = len(cfg.pos)
+        pairs = (len(s.centers) + len(b.centers)) * T
+        # canonical per-pair work: smooth pair (surface) or sequential
+        # refracted pair (bed), taper, rough overhead, and 10 FLOP + 2 MUFU
+        # per series term with the per-facet term count
+        # n_terms_for((2 k_local sigma_i)^2)
+        def terms(k_loc, sig):
+            x = (2.0 * k_loc * np.asarray(sig, np.float64)) ** 2
+            return np.clip(np.ceil(x + 6.0 * np.sqrt(x) + 5.0), 10, 300)
+        n_s_i = terms(k0, rs["sigma"])
+        n_b_i = terms(k0 * np.sqrt(cfg.eps[1]), rb["sigma"])
+        flop = T * (np.sum(47.0 + 6 + 20 + 10 * n_s_i) +
+                    np.sum(pair_flops(1, False) + 6 + 20 + 10 * n_b_i))
+        mufu = T * (np.sum(8.0 + 1 + 3 + 2 * n_s_i) +
+                    np.sum(113.0 + 1 + 3 + 2 * n_b_i))
+        t_fp32 = flop / (peaks["fp32"] * 1e12)
+        t_mufu = mufu / (peaks["mufu_tops"] * 1e12)
+        bound = "mufu" if t_mufu > t_fp32 else "fp32"
+        bands[f"{f0 / 1e6:.0f}MHz"] = {
+            "ms": ms, "kernel_ms": ms_k, "n_terms": [nt_s, nt_b],
+            "n_samples": n_s, "contribs_per_s": pairs / (ms * 1e-3),
+            "roofline": {"bound": bound,
+                         "frac": max(t_fp32, t_mufu) / (ms_k * 1e-3),
+                         "fp32_tflops": flop / (ms_k * 1e-3) / 1e12,
+                         "mufu_tops": mufu / (ms_k * 1e-3) / 1e12,
+                         "mean_terms": [float(n_s_i.mean()),
+                                        float(n_b_i.mean())]}}
         total_ms += ms
         total_pairs += pairs
         del ps, pb
     return {"workload": "rough_surface_bed_512sq_25m_2048tr_4bands",
             "unit": "contribs/s", "value": total_pairs / (total_ms * 1e-3),
-            "ms_per_step": total_ms, "bands": bands}
+            "ms_per_step": total_ms, "bands": bands,
+            "roofline_note": "per band: the slower of the FP32 and MUFU "
+                             "pipes at the canonical per-pair counts (FP32 "
+                             "47 or the sequential refracted pair + 6 taper "
+                             "+ 20 rough + 10 per term; MUFU 8 or 113 + 1 + "
+                             "3 + 2 per term; terms per facet from its "
+                             "sigma) over the kernels' event time, against "
+                             "the FMA and MUFU rates measured in this run"}
 
 
 def row_cfg4(device, n_inst, flush, peaks):
@@ -921,12 +952,14 @@ def run_rows(args, device, peak32):
     rows = {}
     if not want:
         return rows
-    peaks = {"fp32": peak32, "fp64": fp32_peak_tflops(device, fp64=True)}
-    rows["peaks_tflops"] = {**peaks, "source": "FMA probes measured in this "
-                            "run (ss_fp32_fma_probe, ss_fp64_fma_probe)"}
+    peaks = {"fp32": peak32, "fp64": fp32_peak_tflops(device, fp64=True),
+             "mufu_tops": fp32_peak_tflops(device, mufu=True)}
+    rows["peaks_tflops"] = {**peaks, "source": "probes measured in this run "
+                            "(ss_fp32_fma_probe, ss_fp64_fma_probe, "
+                            "ss_mufu_probe)"}
     fns = {"cfg1": lambda: row_cfg1(device, flush, peaks),
            "modef": lambda: row_modef(device, flush, peaks),
-           "cfg3": lambda: row_cfg3(device, flush),
+           "cfg3": lambda: row_cfg3(device, flush, peaks),
            "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,
                                     peaks),
            "cfg5": lambda: row_cfg5(device, flush),
@@ -1000,19 +1033,22 @@ def pair_flops(n_crossed, joint):
 LAYER_PATHS = [(0, False), (1, False), (2, True), (3, True)]
 
 
-def fp32_peak_tflops(device, repeats=5, fp64=False):
-    """FP32 (or FP64) FMA rate of this GPU, measured with the library's
-    probe kernel (best of ``repeats`` launches, TFLOP/s)."""
+def fp32_peak_tflops(device, repeats=5, fp64=False, mufu=False):
+    """FP32 (or FP64) FMA rate of this GPU in TFLOP/s, or with ``mufu`` the
+    MUFU rate in Tops/s, measured with the library's probe kernels (best of
+    ``repeats`` launches)."""
     import ctypes as C
     import torch
     from radar_sounder_simulator_gb300 import _lib
     sms = torch.cuda.get_device_properties(device).multi_processor_count
-    blocks, iters = 8 * sms, (1000 if fp64 else 40000)
+    blocks = 8 * sms
+    iters = 1000 if fp64 else (10000 if mufu else 40000)
     out = torch.empty(blocks * 256, dtype=torch.float64 if fp64 else
                       torch.float32, device=device)
     stream = torch.cuda.current_stream(device)
     L = _lib.lib()
-    probe = L.ss_fp64_fma_probe if fp64 else L.ss_fp32_fma_probe
+    probe = (L.ss_fp64_fma_probe if fp64 else
+             L.ss_mufu_probe if mufu else L.ss_fp32_fma_probe)
 
     def launch():
         _lib.check(probe(blocks, iters, C.c_void_p(out.data_ptr()),
@@ -1027,7 +1063,7 @@ def fp32_peak_tflops(device, repeats=5, fp64=False):
         launch()
         e1.record(stream)
         torch.cuda.synchronize()
-        flop = blocks * 256 * 8 * iters * 2.0
+        flop = blocks * 256 * 8 * iters * (1.0 if mufu else 2.0)
         best = max(best, flop / (e0.elapsed_time(e1) * 1e-3) / 1e12)
     return best
 

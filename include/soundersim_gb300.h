@@ -533,6 +533,12 @@ int ss_fp32_fma_probe(int32_t blocks, int32_t iters, float *out,
 int ss_fp64_fma_probe(int32_t blocks, int32_t iters, double *out,
                       void *stream);
 
+/* MUFU (SFU) throughput probe: blocks CTAs of 256 threads, eight chains of
+ * iters base-2 exponentials each; operations per launch = blocks * 256 * 8
+ * * iters. The roofline denominator of the transcendental-heavy work (the
+ * roughness series). */
+int ss_mufu_probe(int32_t blocks, int32_t iters, float *out, void *stream);
+
 /* Adjoint of windowed trace power (no counterpart in the reference). */
 typedef struct {
   const double *field;       /* (T, n_samples, 2) forward field of the target

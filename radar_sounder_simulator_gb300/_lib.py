@@ -254,6 +254,8 @@ SIGNATURES = {
                                     C.c_size_t, C.c_void_p]),
     "ss_fp32_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
+    "ss_mufu_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
+                                C.c_void_p]),
     "ss_fp64_fma_probe": (C.c_int, [C.c_int32, C.c_int32, C.c_void_p,
                                     C.c_void_p]),
     "ss_version": (C.c_char_p, []),

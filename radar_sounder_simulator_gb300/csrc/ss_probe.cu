@@ -41,7 +41,38 @@ fp64_fma_probe_kernel(int iters, double x, double y, double *out) {
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// MUFU (special function unit) probe: eight independent chains of the
+// base-2 exponential x <- 2^-x (bounded in (0, 1)), one MUFU operation per
+// step. Operations per launch = blocks x threads x 8 x iters.
+__global__ void __launch_bounds__(256)
+mufu_probe_kernel(int iters, float *out) {
+  float a[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) a[j] = 0.001f * (float)(threadIdx.x + j);
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      asm volatile("ex2.approx.ftz.f32 %0, %1;" : "=f"(a[j]) : "f"(-a[j]));
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += a[j];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace ss
+
+extern "C" int ss_mufu_probe(int32_t blocks, int32_t iters, float *out,
+                             void *stream) {
+  using namespace ss;
+  if (blocks <= 0 || iters <= 0 || !out) {
+    set_error("bad probe arguments");
+    return SS_ERR_ARG;
+  }
+  mufu_probe_kernel<<<blocks, 256, 0, static_cast<cudaStream_t>(stream)>>>(
+      iters, out);
+  return cuda_status(cudaGetLastError(), "mufu probe launch");
+}
 
 extern "C" int ss_fp64_fma_probe(int32_t blocks, int32_t iters, double *out,
                                  void *stream) {
