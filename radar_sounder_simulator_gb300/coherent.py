@@ -19,7 +19,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .geometry import cull_plan
+from .geometry import cull_plan, group_within_blocks
 
 TWO_PI = 2.0 * np.pi
 
@@ -232,6 +232,8 @@ def prepare_coherent(positions, u_ct, centers, normals, areas, e1, e2, *, k,
     if gamma_facet and gamma_arr.shape != (n,):
         raise ValueError(f"per-facet gamma shape {gamma_arr.shape} != ({n},)")
     rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
+    if s_arr is not None:     # per-facet rms heights: similar series lengths
+        plan = group_within_blocks(plan, s_arr)   # share a warp
     fac = stage_facets(centers, normals, areas, e1, e2, plan.order, device,
                        gamma=gamma_arr if gamma_facet else None,
                        sigma=s_arr, corr=l_arr, phasors=phasors)

@@ -92,3 +92,24 @@ def _cull_plan_device(s_f, s_t, bs, n_blocks, t0, dt, n_samples, c,
     n_win = int(max(1, int((b_hi - b_lo).max())))
     off = np.minimum(b_lo, n_blocks - n_win).astype(np.int32)
     return CullPlan(order, bs, n_blocks, off, n_win)
+
+
+def group_within_blocks(plan, key):
+    """The plan with its facet order regrouped inside every culling block by
+    ``key`` (per facet, in the caller's facet order): facets of similar key
+    become warp neighbours. Used with per-facet roughness, whose series
+    length grows with the rms height: lanes of a warp then run similar
+    trip counts. Block membership -- and so every trace's window -- is
+    unchanged; only the summation order inside a block moves."""
+    order, bs = plan.order, plan.block_size
+    if isinstance(order, torch.Tensor):
+        k = torch.as_tensor(np.ascontiguousarray(key, np.float64),
+                            device=order.device).index_select(0, order)
+        by_key = torch.sort(k, stable=True)[1]
+        blk = torch.div(by_key, bs, rounding_mode="floor")
+        by_blk = torch.sort(blk, stable=True)[1]
+        return plan._replace(order=order.index_select(0,
+                                                      by_key[by_blk]))
+    k = np.asarray(key, np.float64)[order]
+    perm = np.lexsort((k, np.arange(len(order)) // bs))
+    return plan._replace(order=order[perm])

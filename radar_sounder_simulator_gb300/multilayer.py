@@ -19,7 +19,7 @@ import torch
 from . import _lib
 from .coherent import (_dev, _field_to_host, pattern_struct, permuted,
                        rough_struct, stage_facets, to_host)
-from .geometry import cull_plan
+from .geometry import cull_plan, group_within_blocks
 
 
 def _affine_fit(cen, rc):
@@ -229,6 +229,8 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
                      block_size=bs_req, target_pairs=1 << 18,
                      window_cull=window_cull, device=device)
     rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
+    if s_arr is not None:     # per-facet rms heights: similar series lengths
+        plan = group_within_blocks(plan, s_arr)   # share a warp
     fac = stage_facets(centers, target.normals, target.areas, target.e1,
                        target.e2, plan.order, device, sigma=s_arr,
                        corr=l_arr, phasors=phasors)

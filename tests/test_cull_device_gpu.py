@@ -44,3 +44,22 @@ def test_ties_and_signed_zero_keep_index_order():
         np.testing.assert_array_equal(d.order.cpu().numpy(), h.order)
         np.testing.assert_array_equal(d.off, h.off)
         assert d.n_win == h.n_win
+
+
+def test_regrouping_within_blocks_matches_host(golden):
+    """Facets regrouped by a per-facet key inside each culling block: the
+    device permutation equals the host one, and block membership (every
+    trace's window) is unchanged."""
+    from radar_sounder_simulator_gb300.geometry import group_within_blocks
+    g = golden("coherent")
+    pos, cen = g["pos"], g["surf_centers"]
+    kw = dict(t0=2 * 1400.0 / C, dt=1e-8, n_samples=64, c=C, block_size=64,
+              target_pairs=1 << 12)
+    key = np.random.default_rng(3).lognormal(0, 1, len(cen))
+    key[::7] = key[0]                      # ties keep their order
+    h = group_within_blocks(cull_plan(pos, cen, **kw), key)
+    d = group_within_blocks(cull_plan(pos, cen, device="cuda", **kw), key)
+    np.testing.assert_array_equal(d.order.cpu().numpy(), h.order)
+    base = cull_plan(pos, cen, **kw).order
+    for b in range(0, len(base), 64):
+        assert set(h.order[b:b + 64]) == set(base[b:b + 64])
