@@ -873,6 +873,7 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   __shared__ float s_pat[SS_PAT_MAX];
   __shared__ float s_fad[SS_FAD_N];
   __shared__ int s_rng[2];
+  __shared__ int s_next;
   const int chunk = blockIdx.x;
   const int t_base = blockIdx.y * a.tb;
   const int nt = min(a.tb, a.T - t_base);
@@ -908,10 +909,22 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
     long len = max(hi - lo, 0);
     s_rng[0] = lo + (int)(len * chunk / a.n_chunks);
     s_rng[1] = lo + (int)(len * (chunk + 1) / a.n_chunks);
+    s_next = s_rng[0];
   }
   __syncthreads();
 
-  for (int i = s_rng[0] + tid; i < s_rng[1]; i += blockDim.x) {
+  // warps take 32 consecutive facets at a time from a shared counter, so a
+  // warp whose pairs iterate longer (solver steps, series terms, deferred
+  // decisions) does not hold the others at the write-out barrier
+  const int lane = tid & 31;
+  const int i_end = s_rng[1];
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&s_next, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= i_end) break;
+    const int i = base + lane;
+    if (i >= i_end) continue;
     const float q[3] = {a.F.cx[i], a.F.cy[i], a.F.cz[i]};
     for (int tt = 0; tt < nt; ++tt) {
       if (i < s_lo[tt] || i >= s_hi[tt]) continue;
