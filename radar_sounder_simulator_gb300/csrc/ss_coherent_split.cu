@@ -59,6 +59,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   __shared__ float s_pat[SS_PAT_MAX];
   __shared__ float s_fad[SS_FAD_N];
   __shared__ int s_rng[2];
+  __shared__ int s_next;
 
   const int t_base = group * a.tb;
   const int nt = min(a.tb, a.T - t_base);
@@ -105,6 +106,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
     long len = max(hi - lo, 0);
     s_rng[0] = lo + (int)(len * chunk / a.n_chunks);
     s_rng[1] = lo + (int)(len * (chunk + 1) / a.n_chunks);
+    s_next = s_rng[0];
   }
   __syncthreads();
 
@@ -117,7 +119,17 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   float dropl[SS_MAX_TB];
 #pragma unroll
   for (int j = 0; j < SS_MAX_TB; ++j) dropl[j] = 0.0f;
-  for (int i = s_rng[0] + tid; i < s_rng[1]; i += blockDim.x) {
+  // warps take 32 consecutive facets at a time from a shared counter (the
+  // roughness series makes pair costs uneven)
+  const int lane = tid & 31;
+  const int i_end = s_rng[1];
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = atomicAdd(&s_next, 32);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= i_end) break;
+    const int i = base + lane;
+    if (i >= i_end) continue;
     const float cx = a.F.cx[i], cy = a.F.cy[i], cz = a.F.cz[i];
     const float nx = a.F.nx[i], ny = a.F.ny[i], nz = a.F.nz[i];
     const float e1x = a.F.e1x[i], e1y = a.F.e1y[i], e1z = a.F.e1z[i];
