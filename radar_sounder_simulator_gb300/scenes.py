@@ -127,7 +127,7 @@ def config2(seed=2, n_cells=512, n_traces=1024, spacing=50.0,
     bed at 2500 m, each n_cells^2 facets of ``spacing`` metres; 1024 traces
     at 20 km; 60 MHz / 15 MHz.
 
-    Choices where the configuration is silent (recorded in the design doc):
+    Choices where the configuration is silent:
     horizon ACF exponential with 1 km correlation; bed relief exponential,
     5 km; relative permittivity contrast 1e-3 at both horizons (their target
     reflection coefficient fresnel_normal(eps, eps (1 + 1e-3))); firn column

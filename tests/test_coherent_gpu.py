@@ -2,7 +2,7 @@
 
 FP64 form: within 1e-9 of the oracle per bin (float64 rounding only; the
 binning chain is round-to-nearest, so bins are identical). Split form: the
-spec tolerances -- relative L2 <= 1e-4, phase <= 1e-3 rad and power
+path tolerances -- relative L2 <= 1e-4, phase <= 1e-3 rad and power
 <= 0.01 dB for bins above -60 dB of the peak.
 """
 

@@ -6,7 +6,7 @@ by operation (round-to-nearest, same interpolation, phase and summation
 order), so it matches the golden complex64 field to within one complex64
 rounding (relative 1e-6 of the peak) and the oracle to 1e-12 relative L2.
 The split form computes in float32 (dr without cancellation, phase reduced
-modulo 2 pi): relative L2 <= 1e-4 (the spec float bound) and the
+modulo 2 pi): relative L2 <= 1e-4 (the path's float bound) and the
 power of samples above -60 dB within 0.01 dB."""
 
 import json

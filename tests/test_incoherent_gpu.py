@@ -7,7 +7,7 @@ through the nonzero pattern of one-facet-per-bin cases and of the golden
 histograms. Powers are float32 per pair (the kernel uses a reciprocal square
 root where the reference divides) and summed in float32 per CTA chunk, so
 each histogram is within 1e-5 relative L2 of the reference's and the
-oracle's (the spec float bound is 1e-4)."""
+oracle's (the path's float bound is 1e-4)."""
 
 import numpy as np
 import pytest

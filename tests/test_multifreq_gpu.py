@@ -4,7 +4,7 @@ Against the reference's own outputs (golden, float64 facets) and the
 float64 oracle on the same float32-quantised facets the kernels read:
 FP64 form within 1e-9 of the profile peak (oracle) / 1e-6 (golden, which
 differs by the float32 facet quantisation); split form within the
-spec bounds -- relative L2 <= 1e-4, phase <= 1e-3 rad, power within
+path bounds -- relative L2 <= 1e-4, phase <= 1e-3 rad, power within
 0.01 dB for samples above -60 dB of the peak.
 """
 

@@ -6,7 +6,7 @@ Tolerances: the GPU convolves the float32-rounded input (the reference
 convolves the kernels' complex64 output) with compensated float32 sums and
 writes complex64, so each output sample is within a few float32 roundings
 of the float64 result: absolute error <= 3e-7 of the row peak against the
-oracle on the same (rounded) input, and the benchmark spec's bound -- power within
+oracle on the same (rounded) input, and the path's bound -- power within
 0.01 dB -- for every sample above -60 dB of the peak.
 """
 
