@@ -80,3 +80,44 @@ def test_struct_layouts_match_header(tmp_path):
         for fname, _ in py._fields_:
             assert int(out[f"{cname}.{fname}"]) == getattr(py, fname).offset, \
                 f"{cname}.{fname}"
+
+
+def test_c_program_links_and_calls_host_entry_points(tmp_path):
+    """A plain C program includes the header, links libsoundercuda.so and
+    calls entry points that need no GPU (build string, scratch sizing,
+    argument validation) -- the binding a C or cgo caller would use."""
+    import shutil
+    import subprocess
+    import pytest
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    build.build()
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    src = tmp_path / "caller.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include <string.h>
+#include "soundersim_gb300.h"
+int main(void) {
+  ss_incoherent_opts o;
+  memset(&o, 0, sizeof o);
+  o.t0 = 1e-5; o.dt = 1e-8; o.c = 299792458.0; o.n_samples = 128;
+  size_t n = ss_incoherent_scratch_bytes(&o, 64, 100000);
+  ss_focus_opts f;
+  memset(&f, 0, sizeof f);
+  f.n_traces = 10; f.n_bins = 100;
+  size_t nf = ss_focused_sar_scratch_bytes(&f);
+  int st = ss_incoherent_fwd(NULL, NULL, NULL, NULL, NULL, NULL, 0, NULL);
+  printf("%s|%zu|%zu|%d|%s\n", ss_version(), n, nf, st, ss_last_error());
+  return 0;
+}
+""")
+    exe = tmp_path / "caller"
+    subprocess.run(["gcc", f"-I{os.path.join(ROOT, 'include')}", str(src),
+                    f"-L{libdir}", "-lsoundercuda", f"-Wl,-rpath,{libdir}",
+                    "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True,
+                         check=True).stdout.strip().split("|")
+    assert "sm_103a" in out[0]
+    assert int(out[1]) > 0 and int(out[2]) == 10 * 8 + 100 * 16
+    assert int(out[3]) == 1 and "null argument" in out[4]
