@@ -24,7 +24,8 @@ __device__ __forceinline__ double dot3v(const double *a, const double *b) {
 // form of multilayer.py:196-266).
 static __device__ __noinline__ void snell64(const double *p, const double *q, const double *o,
                         const double *nrm, double n1, double n2, int n_iter,
-                        bool comp, Snell64 &R, bool early = false) {
+                        bool comp, Snell64 &R, bool early = false,
+                        bool x_only = false) {
   double po[3] = {p[0] - o[0], p[1] - o[1], p[2] - o[2]};
   double qo[3] = {q[0] - o[0], q[1] - o[1], q[2] - o[2]};
   const double h1 = dot3v(po, nrm), h2 = dot3v(qo, nrm);
@@ -73,6 +74,11 @@ static __device__ __noinline__ void snell64(const double *p, const double *q, co
   const double c1 = fmax((1.0 - sig) * (1.0 + sig), kTiny);
   const double tr = comp ? ar * sig * (1.0 / sqrt(c1)) : ar * sig / sqrt(c1);
   const double t = fmin(fmax(swap ? Lh - tr : tr, 0.0), Lh);
+  if (x_only) {  // the crossing point alone (lookup anchors)
+    const double st = s * t;
+    for (int j = 0; j < 3; ++j) R.x[j] = fp[j] + st * u[j];
+    return;
+  }
   const double d2 = Lh - t;
   const double r1 = fmax(sqrt(ah * ah + t * t), kTiny);
   const double r2 = fmax(sqrt(bh * bh + d2 * d2), kTiny);

@@ -197,7 +197,8 @@ static __device__ __noinline__ void cell64(const ss_interface &I, const double *
                                     bool comp, double *x_out, int &row,
                                     int &col) {
   Snell64 R;
-  snell64(cur, q, I.mean_point, I.mean_normal, n1, n2, 10, comp, R, true);
+  snell64(cur, q, I.mean_point, I.mean_normal, n1, n2, 10, comp, R, true,
+          true);
   const double rc0 = __dadd_rn(__dadd_rn(__dmul_rn(R.x[0], I.coef[0]),
                                          __dmul_rn(R.x[1], I.coef[2])),
                                I.coef[4]);
