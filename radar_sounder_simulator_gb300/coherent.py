@@ -224,14 +224,19 @@ def prepare_coherent(positions, u_ct, centers, normals, areas, e1, e2, *, k,
     pos = np.asarray(positions, np.float64)
     T = len(pos)
     n = np.asarray(centers).shape[0]
-    plan = cull_plan(pos, centers, t0=t0, dt=dt, n_samples=n_samples, c=c,
-                     block_size=block_size, target_pairs=1 << 19,
-                     window_cull=window_cull, device=device)
+    # argument errors come before any device work, as in the reference
+    if precision not in _lib.PREC:
+        raise ValueError(f"unknown precision {precision!r}")
     gamma_arr = np.asarray(gamma, np.float32)
     gamma_facet = gamma_arr.ndim > 0
     if gamma_facet and gamma_arr.shape != (n,):
         raise ValueError(f"per-facet gamma shape {gamma_arr.shape} != ({n},)")
     rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
+    if pattern is not None and pattern[0] not in _lib.PATTERN:
+        raise ValueError(f"unknown pattern kind {pattern[0]!r}")
+    plan = cull_plan(pos, centers, t0=t0, dt=dt, n_samples=n_samples, c=c,
+                     block_size=block_size, target_pairs=1 << 19,
+                     window_cull=window_cull, device=device)
     if s_arr is not None:     # per-facet rms heights: similar series lengths
         plan = group_within_blocks(plan, s_arr)   # share a warp
     fac = stage_facets(centers, normals, areas, e1, e2, plan.order, device,

@@ -68,6 +68,8 @@ def prepare_incoherent(positions, u_ct, centers, normals, areas, *, t0, dt,
     device = torch.device(device or "cuda")
     if int(block_size) <= 0:
         raise ValueError(f"block_size must be positive, got {block_size}")
+    if pattern is not None and pattern[0] not in _lib.PATTERN:
+        raise ValueError(f"unknown pattern kind {pattern[0]!r}")
     pos = np.asarray(positions, np.float64).reshape(-1, 3)
     T = len(pos)
     n = np.asarray(centers).shape[0]

@@ -121,6 +121,16 @@ def prepare_multifreq(positions, centers, normals, areas, e1, e2, *, gamma,
     tw = np.asarray(twtt, np.float64).ravel()
     T, B = len(pos), len(tw)
     n = np.asarray(centers).shape[0]
+    # option errors come before any device work
+    if precision not in _lib.PREC:
+        raise ValueError(f"unknown precision {precision!r}")
+    if roughness is not None and not freeze_amplitudes:
+        raise ValueError("roughness needs freeze_amplitudes=True")
+    gamma_arr = np.asarray(gamma, np.float32)
+    gamma_facet = gamma_arr.ndim > 0
+    if gamma_facet and gamma_arr.shape != (n,):
+        raise ValueError(f"per-facet gamma shape {gamma_arr.shape} != ({n},)")
+    rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
     if check_alias:
         span = _delay_span(pos, centers, tw, c, device)
         if span > n_freq / bandwidth:
@@ -128,17 +138,10 @@ def prepare_multifreq(positions, centers, normals, areas, e1, e2, *, gamma,
                 f"multifreq referee would alias: delay span {span * 1e6:.2f} "
                 f"us > K/B = {n_freq / bandwidth * 1e6:.2f} us; raise n_freq "
                 "or shrink the scene/window")
-    if roughness is not None and not freeze_amplitudes:
-        raise ValueError("roughness needs freeze_amplitudes=True")
     dt = (tw[-1] - tw[0]) / max(B - 1, 1) if B > 1 else 1e-9
     plan = cull_plan(pos, centers, t0=tw[0], dt=dt, n_samples=B, c=c,
                      block_size=block_size, target_pairs=1 << 19,
                      window_cull=window_cull)
-    gamma_arr = np.asarray(gamma, np.float32)
-    gamma_facet = gamma_arr.ndim > 0
-    if gamma_facet and gamma_arr.shape != (n,):
-        raise ValueError(f"per-facet gamma shape {gamma_arr.shape} != ({n},)")
-    rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
     fac = stage_facets(centers, normals, areas, e1, e2, plan.order, device,
                        gamma=gamma_arr if gamma_facet else None,
                        sigma=s_arr, corr=l_arr, phasors=phasors)

@@ -181,6 +181,22 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
     gamma_facet = gamma_arr.ndim > 0
     if gamma_facet and not coherent:
         raise ValueError("per-facet gamma requires coherent mode")
+    if precision not in _lib.PREC:
+        raise ValueError(f"unknown precision {precision!r}")
+    # the remaining argument errors also come before any device work
+    n = np.asarray(target.centers).shape[0]
+    rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
+    if diffuse is not None:
+        if not coherent:
+            raise ValueError("diffuse channel requires coherent mode")
+        d_amp = np.asarray(diffuse[0], np.float64)
+        if d_amp.shape != (n,):
+            raise ValueError(f"diffuse amp shape {d_amp.shape} != ({n},)")
+    if gamma_facet and gamma_arr.shape != (n,):
+        raise ValueError(f"per-facet gamma shape {gamma_arr.shape} != "
+                         f"({n},)")
+    if pattern is not None and pattern[0] not in _lib.PATTERN:
+        raise ValueError(f"unknown pattern kind {pattern[0]!r}")
     eps = np.asarray(eps_leg, np.float64)
     n_leg = np.sqrt(eps)
     att = np.asarray(att_leg, np.float64)
@@ -202,12 +218,12 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
         att = np.concatenate([np.full(k_pad, att[0]), att])
         if sig_c is not None:
             sig_c = np.concatenate([np.zeros(k_pad), sig_c])
-    ifaces += [grid_consts_device(f, device) for f in crossed]
-    ni = len(ifaces)
+    ni = k_pad + len(crossed)
     if not 1 <= ni <= 8:
         raise ValueError(f"{ni} crossed interfaces; the kernel takes 1..8")
     if len(n_leg) < ni + 1 or (joint and len(n_leg) != ni + 1):
         raise ValueError("eps_leg/att_leg need len(crossed) + 1 entries")
+    ifaces += [grid_consts_device(f, device) for f in crossed]
     arr = (_lib.Interface * ni)()
     for j, (tab, coef, mp, mn) in enumerate(ifaces):
         t = (tab if isinstance(tab, torch.Tensor)
@@ -223,12 +239,10 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
                else None)
 
     centers = np.asarray(target.centers)
-    n = centers.shape[0]
     bs_req = block_size or (4096 if joint else None)
     plan = cull_plan(pos, centers, t0=t0, dt=dt, n_samples=n_samples, c=c,
                      block_size=bs_req, target_pairs=1 << 18,
                      window_cull=window_cull, device=device)
-    rst, s_arr, l_arr, phasors = rough_struct(roughness, d_phi_area)
     if s_arr is not None:     # per-facet rms heights: similar series lengths
         plan = group_within_blocks(plan, s_arr)   # share a warp
     fac = stage_facets(centers, target.normals, target.areas, target.e1,
@@ -236,12 +250,7 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
                        corr=l_arr, phasors=phasors)
     n_exp = 0.0
     if diffuse is not None:
-        if not coherent:
-            raise ValueError("diffuse channel requires coherent mode")
-        d_amp, d_ph, n_exp = diffuse
-        d_amp = np.asarray(d_amp, np.float64)
-        if d_amp.shape != (n,):
-            raise ValueError(f"diffuse amp shape {d_amp.shape} != ({n},)")
+        _, d_ph, n_exp = diffuse
         fac.extras["diffuse_amp"] = permuted(d_amp, np.float64, plan.order,
                                              device)
         fac.extras["diffuse_phasor"] = permuted(
@@ -249,9 +258,6 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
                 np.float32).reshape(n, 2), np.float32, plan.order,
             device).reshape(-1)
     if gamma_facet:
-        if gamma_arr.shape != (n,):
-            raise ValueError(f"per-facet gamma shape {gamma_arr.shape} != "
-                             f"({n},)")
         fac.extras["gamma_f64"] = permuted(gamma_arr, np.float64,
                                            plan.order, device)
     pst, pv_t, pv_len, pkeep = pattern_struct(pattern, T, device)
