@@ -121,3 +121,38 @@ int main(void) {
     assert "sm_103a" in out[0]
     assert int(out[1]) > 0 and int(out[2]) == 10 * 8 + 100 * 16
     assert int(out[3]) == 1 and "null argument" in out[4]
+
+
+def _null_call_cases():
+    import ctypes as C
+    for name, (res, args) in sorted(_lib.SIGNATURES.items()):
+        if res is C.c_size_t or name in ("ss_version", "ss_last_error",
+                                         "ss_refracted_adjoint_blocks"):
+            continue
+        yield name, args
+
+
+def test_every_entry_point_rejects_null_arguments():
+    """Each status-returning entry point answers null pointers with
+    SS_ERR_ARG and a message, before any CUDA call, and the Python side maps
+    that status to ValueError (the reference's exception type for argument
+    errors). Sizes are 1, so an empty call cannot pass as a no-op. Runs only
+    on a host without a GPU, where no call can reach a launch."""
+    import ctypes as C
+    import pytest
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("host-only check; the GPU suite covers device calls")
+    build.build()
+    L = _lib.lib()
+    seen = 0
+    for name, args in _null_call_cases():
+        vals = [1 if a in (C.c_int32, C.c_int64, C.c_uint64, C.c_size_t)
+                else 0.0 if a is C.c_double else None for a in args]
+        st = getattr(L, name)(*vals)
+        assert st == _lib.SS_ERR_ARG, (name, st)
+        assert L.ss_last_error(), name
+        with pytest.raises(ValueError):
+            _lib.check(st, name)
+        seen += 1
+    assert seen >= 20
