@@ -156,3 +156,25 @@ def test_every_entry_point_rejects_null_arguments():
             _lib.check(st, name)
         seen += 1
     assert seen >= 20
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """Without the built library every entry point raises: there is no CPU
+    fallback to fall into."""
+    import numpy as np
+    import pytest
+    from radar_sounder_simulator_gb300.coherent import prepare_coherent
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "absent.so"))
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(_lib.LibraryMissing, match="no CPU"):
+        _lib.lib()
+    c = np.array([[0.0, 0.0, 0.0]])
+    plan = prepare_coherent(np.array([[0.0, 0.0, 100.0]]),
+                            np.array([[0.0, -1.0, 0.0]]), c,
+                            np.array([[0.0, 0.0, 1.0]]), np.ones(1),
+                            np.array([[1.0, 0.0, 0.0]]),
+                            np.array([[0.0, 1.0, 0.0]]), k=1.0, gamma=-0.3,
+                            t0=0.0, dt=1e-8, n_samples=128, c=3e8,
+                            device="cpu")
+    with pytest.raises(_lib.LibraryMissing):
+        plan.run()
