@@ -564,7 +564,7 @@ def row_modef(device, flush, peaks):
             "error_vs_fp64": _errors(res["split"], res["fp64"])}
 
 
-def row_cfg3(device, flush, peaks):
+def row_cfg3(device, flush, peaks, cfg3_error_traces=32):
     """Rough surface and bed, four bands: per band the surface coherent sum
     and the refracted bed sum (per-facet sigma, l; exponential ACF with the
     area-only series and taper), each pulse-compressed."""
@@ -588,18 +588,22 @@ def row_cfg3(device, flush, peaks):
         nt_s = scenes.n_terms_for((2 * k0 * rs["sigma"].max()) ** 2)
         nt_b = scenes.n_terms_for((2 * k0 * np.sqrt(3.15) *
                                    np.quantile(rb["sigma"], 0.999)) ** 2)
-        ps = prepare_coherent(
-            cfg.pos, cfg.uct, s.centers, s.normals, s.areas, s.e1, s.e2,
-            k=k0, gamma=cfg.gamma_surface, t0=t0, dt=dt, n_samples=n_s, c=c,
-            roughness=(rs["sigma"], rs["corr"], rs["phasors"], nt_s,
-                       "exponential"), d_phi_area=True, taper_s=0.05,
-            precision="split", device=device)
-        pb = prepare_refracted(
-            cfg.pos, cfg.uct, b, [s], cfg.eps, cfg.att, mode="coherent",
-            t0=t0, dt=dt, n_samples=n_s, c=c, gamma=cfg.gamma_bed, k0=k0,
-            roughness=(rb["sigma"], rb["corr"], rb["phasors"], nt_b,
-                       "exponential"), d_phi_area=True, taper_s=0.05,
-            refraction="sequential", precision="split", device=device)
+
+        def plans(pos, uct):
+            ps = prepare_coherent(
+                pos, uct, s.centers, s.normals, s.areas, s.e1, s.e2, k=k0,
+                gamma=cfg.gamma_surface, t0=t0, dt=dt, n_samples=n_s, c=c,
+                roughness=(rs["sigma"], rs["corr"], rs["phasors"], nt_s,
+                           "exponential"), d_phi_area=True, taper_s=0.05,
+                precision="split", device=device)
+            pb = prepare_refracted(
+                pos, uct, b, [s], cfg.eps, cfg.att, mode="coherent", t0=t0,
+                dt=dt, n_samples=n_s, c=c, gamma=cfg.gamma_bed, k0=k0,
+                roughness=(rb["sigma"], rb["corr"], rb["phasors"], nt_b,
+                           "exponential"), d_phi_area=True, taper_s=0.05,
+                refraction="sequential", precision="split", device=device)
+            return ps, pb
+        ps, pb = plans(cfg.pos, cfg.uct)
         pulse, m = compressed_pulse(bw, 10e-6, dt, "hann", "chirp")
 
         def step():
@@ -636,6 +640,20 @@ def row_cfg3(device, flush, peaks):
                          "mufu_tops": mufu / (ms_k * 1e-3) / 1e12,
                          "mean_terms": [float(n_s_i.mean()),
                                         float(n_b_i.mean())]}}
+        # split form against the FP64 form on the central traces (both
+        # targets' binned fields); a failure here is reported in the band
+        try:
+            mid = len(cfg.pos) // 2
+            sub = slice(mid - cfg3_error_traces // 2,
+                        mid + cfg3_error_traces // 2)
+            qs, qb = plans(cfg.pos[sub], cfg.uct[sub])
+            outs = [qs.run(), qb.run()]
+            outs64 = [qs.run("fp64"), qb.run("fp64")]
+            err = {"traces": cfg3_error_traces, **split_error(outs, outs64)}
+            del qs, qb, outs, outs64
+        except Exception as exc:  # reported, not hidden
+            err = {"error": f"{type(exc).__name__}: {exc}"}
+        bands[f"{f0 / 1e6:.0f}MHz"]["error_vs_fp64"] = err
         total_ms += ms
         total_pairs += pairs
         del ps, pb
