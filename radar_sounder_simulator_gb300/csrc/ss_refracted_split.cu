@@ -28,6 +28,8 @@ RefSplitConsts split_consts(const RefArgs &a) {
   k.Al = A.lo;
   k.Bh = B.hi;
   k.Bl = B.lo;
+  k.bin_guard = (float)std::max((double)kBinGuard,
+                                kOplGuard * 2.0 / (a.c * a.dt));
   for (int i = 0; i <= a.leg_last; ++i) {
     const df n = df_from_double(a.n_leg[i]);
     k.n_leg[i] = n.hi;

@@ -21,9 +21,12 @@
 //     the lookups are the reference's integer decisions;
 //   * leg lengths, optical path, carrier phase (2 k0 opl mod 2 pi) and the
 //     fast-time bin in double-float. The optical path is stationary in the
-//     crossing positions (Fermat), so their float32 error enters at second
-//     order; a pair within 1e-6 of a bin edge is re-evaluated with the
-//     complete float64 path, so bins equal the float64 form's;
+//     crossing positions along the interface (Fermat), so that float32
+//     error enters at second order; the crossing's micrometre offset from
+//     the facet plane enters at first order. A pair whose bin position lies
+//     within 5e-5 m of optical path (at least 1e-6 bins) of a bin edge is
+//     re-evaluated with the complete float64 path, so bins equal the float64
+//     form's also for the fine bins of the high bands;
 //   * radiometry (Fresnel, spreading, attenuation, antenna gain, sinc,
 //     roughness series, diffuse channel) in float32.
 //
@@ -44,7 +47,11 @@ constexpr float kTiny32 = 1e-30f;
 constexpr float kEps32 = 1.1920929e-07f;
 constexpr float kTol32 = 1e-4f;
 constexpr float kLookupGuard = 3e-4f;
+// Bin-edge band: the larger of kBinGuard bins and kOplGuard metres of
+// optical path (several times the float32 crossing's first-order
+// optical-path error through up to four crossings).
 constexpr float kBinGuard = 1e-6f;
+constexpr double kOplGuard = 5e-5;
 
 // Per-interface constants of the float32 lookup pass.
 struct MeanPlane32 {
@@ -61,6 +68,7 @@ struct RefSplitConsts {
   float k0, amp_pref_j, kj, taper_inv, sigma, corr, fadL, n_exp;
   float K2h, K2l;             // 2 k0 as double-float
   float Ah, Al, Bh, Bl;       // u = opl A - B, A = 2/(c dt), B = t0/dt
+  float bin_guard;            // bin-edge band in bins (kBinGuard, kOplGuard)
   float n_leg[SS_MAX_IFACE + 1], n_leg_lo[SS_MAX_IFACE + 1],
       eps_leg[SS_MAX_IFACE + 1], att_leg[SS_MAX_IFACE + 1],
       sig_c[SS_MAX_IFACE];
@@ -829,7 +837,7 @@ __device__ __forceinline__ bool pair_eval(
   float frac = (us - fb) + ul;
   if (frac < 0.0f) { fb -= 1.0f; frac += 1.0f; }
   else if (frac >= 1.0f) { fb += 1.0f; frac -= 1.0f; }
-  if ((frac < kBinGuard || frac > 1.0f - kBinGuard) && us > -4.0f &&
+  if ((frac < k.bin_guard || frac > 1.0f - k.bin_guard) && us > -4.0f &&
       us < nsf + 4.0f) {
     if (!EXACT) return false;
     bool v64;
