@@ -12,8 +12,10 @@
 //     the long platform offset p - o formed exactly as a double-float and
 //     rounded once. The crossing is rebuilt from the short side of the ray
 //     (the target's foot for a downward ray), so the float32 root places the
-//     crossing to micrometres, which keeps the facet's arrival direction --
-//     and the sinc arguments k_j (r_hat . e) -- accurate to ~1e-8 rad;
+//     crossing to micrometres near the facet centre (to ~3e-5 m where a
+//     steep facet's plane meets the ray hundreds of metres from its
+//     centre), which keeps the facet's arrival direction -- and the sinc
+//     arguments k_j (r_hat . e) -- accurate to ~1e-8 rad;
 //   * facet lookups: the float32 mean-plane crossing gives the affine cell
 //     coordinate (formed as a double-float; the crossing itself carries
 //     ~2e-5 cells of float32 error); within 3e-4 cells of a rounding boundary the
@@ -22,11 +24,12 @@
 //   * leg lengths, optical path, carrier phase (2 k0 opl mod 2 pi) and the
 //     fast-time bin in double-float. The optical path is stationary in the
 //     crossing positions along the interface (Fermat), so that float32
-//     error enters at second order; the crossing's micrometre offset from
-//     the facet plane enters at first order. A pair whose bin position lies
-//     within 5e-5 m of optical path (at least 1e-6 bins) of a bin edge is
-//     re-evaluated with the complete float64 path, so bins equal the float64
-//     form's also for the fine bins of the high bands;
+//     error enters at second order; the crossing's float32 offset from the
+//     facet plane (up to ~1e-5 m for far crossings) enters at first order.
+//     A pair whose bin position lies within 5e-5 m of optical path (at
+//     least 1e-6 bins) of a bin edge is re-evaluated with the complete
+//     float64 path, so bins equal the float64 form's also for the fine bins
+//     of the high bands;
 //   * radiometry (Fresnel, spreading, attenuation, antenna gain, sinc,
 //     roughness series, diffuse channel) in float32.
 //
