@@ -5,7 +5,6 @@ rate counts every rank's pairs over the slowest rank's time. No GPU."""
 import os
 import socket
 
-import numpy as np
 import pytest
 import torch
 import torch.distributed as dist
