@@ -73,3 +73,12 @@ def test_local_frame_matches_oracle():
     x = np.array([[1000.0, -2000.0, 50.0]])
     np.testing.assert_allclose(fr.local_to_ecef(x), of.local_to_ecef(x),
                                atol=1e-8)
+
+
+def test_series_length_matches_reference(golden):
+    """The series length the benchmark scenes pick follows the reference's
+    n_terms_for (roughness.py:189-196), checked against its outputs."""
+    from radar_sounder_simulator_gb300 import scenes
+    g = golden("primitives")
+    assert [scenes.n_terms_for(x) for x in g["nterms_x"]] == list(
+        g["nterms"])
