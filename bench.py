@@ -642,18 +642,20 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32):
                                         float(n_b_i.mean())]}}
         # split form against the FP64 form on the central traces (both
         # targets' binned fields); a failure here is reported in the band
-        try:
-            mid = len(cfg.pos) // 2
-            sub = slice(mid - cfg3_error_traces // 2,
-                        mid + cfg3_error_traces // 2)
-            qs, qb = plans(cfg.pos[sub], cfg.uct[sub])
-            outs = [qs.run(), qb.run()]
-            outs64 = [qs.run("fp64"), qb.run("fp64")]
-            err = {"traces": cfg3_error_traces, **split_error(outs, outs64)}
-            del qs, qb, outs, outs64
-        except Exception as exc:  # reported, not hidden
-            err = {"error": f"{type(exc).__name__}: {exc}"}
-        bands[f"{f0 / 1e6:.0f}MHz"]["error_vs_fp64"] = err
+        if cfg3_error_traces:
+            try:
+                mid = len(cfg.pos) // 2
+                sub = slice(mid - cfg3_error_traces // 2,
+                            mid + cfg3_error_traces // 2)
+                qs, qb = plans(cfg.pos[sub], cfg.uct[sub])
+                outs = [qs.run(), qb.run()]
+                outs64 = [qs.run("fp64"), qb.run("fp64")]
+                err = {"traces": cfg3_error_traces,
+                       **split_error(outs, outs64)}
+                del qs, qb, outs, outs64
+            except Exception as exc:  # reported, not hidden
+                err = {"error": f"{type(exc).__name__}: {exc}"}
+            bands[f"{f0 / 1e6:.0f}MHz"]["error_vs_fp64"] = err
         total_ms += ms
         total_pairs += pairs
         del ps, pb
@@ -977,7 +979,8 @@ def run_rows(args, device, peak32):
                             "ss_mufu_probe)"}
     fns = {"cfg1": lambda: row_cfg1(device, flush, peaks),
            "modef": lambda: row_modef(device, flush, peaks),
-           "cfg3": lambda: row_cfg3(device, flush, peaks),
+           "cfg3": lambda: row_cfg3(device, flush, peaks,
+                                    0 if args.skip_fp64 else 32),
            "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,
                                     peaks),
            "cfg5": lambda: row_cfg5(device, flush),
