@@ -1,0 +1,57 @@
+"""The benchmark's roofline and error arithmetic, on CPU: the canonical
+per-pair FLOP counts the roofline divides by, and the split-vs-FP64 error
+measures (relative L2, max phase and max dB over bins above -60 dB)."""
+
+import numpy as np
+import pytest
+import torch
+
+import bench
+
+
+def test_canonical_pair_flops():
+    # smooth pair (coherent.py:107-128 + binning), one sequential crossing
+    # (35 Snell iterations of 20 + lookup / plane / Fresnel 60, radiometry),
+    # and the joint path through three crossings at the default budgets
+    assert bench.pair_flops(0, False) == 47.0
+    assert bench.pair_flops(1, False) == 865.0
+    assert bench.pair_flops(2, False) == 1650.0
+    assert bench.pair_flops(3, True) == 11135.0
+    assert bench.pair_flops(2, True) > 2 * bench.pair_flops(2, False)
+
+
+def _field(T, B, seed):
+    g = torch.Generator().manual_seed(seed)
+    return torch.randn(T, B, 2, dtype=torch.float64, generator=g)
+
+
+def test_split_error_measures():
+    f = _field(4, 64, 0)
+    zero = bench.split_error([(f, None)], [(f.clone(), None)])
+    assert zero["rel_l2"] == 0.0
+    assert zero["phase_rad"] < 1e-15 and zero["power_db"] < 1e-12
+    # a pure phase rotation of 1e-3 rad: rel L2 ~ 1e-3, phase 1e-3, 0 dB
+    c = torch.view_as_complex(f.contiguous())
+    rot = torch.view_as_real(c * np.exp(1j * 1e-3))
+    e = bench.split_error([(rot, None)], [(f, None)])
+    assert e["rel_l2"] == pytest.approx(1e-3, rel=1e-3)
+    assert e["phase_rad"] == pytest.approx(1e-3, rel=1e-6)
+    assert e["power_db"] < 1e-9
+    # a gain of 0.01 dB in amplitude squared on every bin
+    g = 10 ** (0.01 / 20)
+    e = bench.split_error([(f * g, None)], [(f, None)])
+    assert e["power_db"] == pytest.approx(0.01, rel=1e-6)
+    # the worst layer is reported
+    e2 = bench.split_error([(f, None), (f * g, None)],
+                           [(f, None), (f, None)])
+    assert e2["power_db"] == pytest.approx(0.01, rel=1e-6)
+
+
+def test_errors_ignore_bins_below_minus_60_db():
+    b = torch.ones(8, dtype=torch.complex128)
+    b[3] = 1e-4                      # -80 dB: outside the measured set
+    a = b.clone()
+    a[3] = -1e-4                     # pi rad off, but not counted
+    e = bench._errors(a, b)
+    assert e["phase_rad"] == 0.0 and e["power_db"] == 0.0
+    assert e["rel_l2"] > 0.0
