@@ -221,18 +221,35 @@ static __device__ __noinline__ void cell64(const ss_interface &I, const double *
   for (int j = 0; j < 3; ++j) x_out[j] = R.x[j];
 }
 
+// Plane point o and unit normal n of a table cell; t (optional) receives
+// the normal as stored, whose direction the float64 form uses.
 __device__ __forceinline__ void cell_plane32(const ss_interface &I, int row,
-                                             int col, float *o, float *n) {
+                                             int col, float *o, float *n,
+                                             float *t = nullptr) {
   const float *g = I.table + ((size_t)row * I.nx + col) * 6;
   for (int j = 0; j < 3; ++j) {
     o[j] = g[j];
     n[j] = g[3 + j];
+    if (t) t[j] = n[j];
   }
   // unit length to float32 rounding (rsqrt seed + one Newton step)
   const float nn = dot3a(n, n);
   float in = rsqrtf(nn);
   in = in * __fmaf_rn(-0.5f * nn * in, in, 1.5f);
   for (int j = 0; j < 3; ++j) n[j] *= in;
+}
+
+// t . y from exact products (two_prod) and a compensated sum: the height of
+// a float32 point y (relative to the plane point) over the plane of normal
+// t, to float32 precision of the height itself.
+__device__ __forceinline__ float plane_height(const float *y, const float *t) {
+  float p0, e0, p1, e1, p2, e2, s, f1, f2;
+  two_prod(y[0], t[0], p0, e0);
+  two_prod(y[1], t[1], p1, e1);
+  two_prod(y[2], t[2], p2, e2);
+  two_sum(p0, p1, s, f1);
+  two_sum(s, p2, s, f2);
+  return s + ((f1 + f2) + (e0 + e1 + e2));
 }
 
 __device__ __forceinline__ float fresnel_gamma32(float e1, float e2,
@@ -310,8 +327,8 @@ __device__ __forceinline__ void path_sequential_split(const RefArgs &a,
         cur64[j] = i == 0 ? p64[j] : (double)o_prev[j] + (double)y_prev[j];
       cell64(I, cur64, q64, a.n_leg[i], a.n_leg[i + 1], true, x1, row, col);
     }
-    float o[3], n[3];
-    cell_plane32(I, row, col, o, n);
+    float o[3], n[3], tn[3];
+    cell_plane32(I, row, col, o, n, tn);
     // local-plane solve relative to the facet centre o
     if (i == 0) {
       p_minus(T, o, Pd);
@@ -330,6 +347,18 @@ __device__ __forceinline__ void path_sequential_split(const RefArgs &a,
     const df s1 = df_norm3(df_add_f(Pd[0], -y[0]), df_add_f(Pd[1], -y[1]),
                            df_add_f(Pd[2], -y[2]));
     P.opl = df_add(P.opl, df_mul(s1, df_make(k.n_leg[i], k.n_leg_lo[i])));
+    // A crossing hundreds of metres from its facet centre carries ~3e-5 m
+    // of float32 rounding, ~1e-5 m of it off the facet plane, which the
+    // optical path takes at first order (the in-plane part is second
+    // order). Moving the crossing onto the plane of the table's own normal
+    // changes the two legs by hp c1 and -hp c2, hp its height over that
+    // plane towards the upper point.
+    {
+      const float hp = dot3a(Ph, n) >= 0.0f ? plane_height(y, tn)
+                                            : -plane_height(y, tn);
+      P.opl = df_add_f(P.opl, hp * (k.n_leg[i] * S.c1 -
+                                    k.n_leg[i + 1] * S.c2));
+    }
     const float c_inc = fmaxf(S.c1, (float)kCMin);
     if (i == 0) {
       P.c0 = c_inc;
