@@ -25,8 +25,10 @@
 //     fast-time bin in double-float. The optical path is stationary in the
 //     crossing positions along the interface (Fermat), so that float32
 //     error enters at second order; the crossing's float32 offset from the
-//     facet plane (up to ~1e-5 m for far crossings) enters at first order.
-//     A pair whose bin position lies within 5e-5 m of optical path (at
+//     facet plane (up to ~1e-5 m for far crossings) enters at first order,
+//     and the sequential path adds it back (height from exact products
+//     times the legs' index-weighted cosines). A pair whose bin position
+//     lies within 5e-5 m of optical path (at
 //     least 1e-6 bins) of a bin edge is re-evaluated with the complete
 //     float64 path, so bins equal the float64 form's also for the fine bins
 //     of the high bands;
@@ -352,7 +354,10 @@ __device__ __forceinline__ void path_sequential_split(const RefArgs &a,
     // optical path takes at first order (the in-plane part is second
     // order). Moving the crossing onto the plane of the table's own normal
     // changes the two legs by hp c1 and -hp c2, hp its height over that
-    // plane towards the upper point.
+    // plane towards the upper point. c2 is the two-point solve's cosine
+    // towards the target: exact for the last crossing; for an upper
+    // crossing of a chain the next leg bends at the next interface, so
+    // that half of the correction is approximate there.
     {
       const float hp = dot3a(Ph, n) >= 0.0f ? plane_height(y, tn)
                                             : -plane_height(y, tn);
