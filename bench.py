@@ -589,17 +589,17 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32):
         nt_b = scenes.n_terms_for((2 * k0 * np.sqrt(3.15) *
                                    np.quantile(rb["sigma"], 0.999)) ** 2)
 
-        def plans(pos, uct):
+        def plans(pos, uct, nts=nt_s, ntb=nt_b):
             ps = prepare_coherent(
                 pos, uct, s.centers, s.normals, s.areas, s.e1, s.e2, k=k0,
                 gamma=cfg.gamma_surface, t0=t0, dt=dt, n_samples=n_s, c=c,
-                roughness=(rs["sigma"], rs["corr"], rs["phasors"], nt_s,
+                roughness=(rs["sigma"], rs["corr"], rs["phasors"], nts,
                            "exponential"), d_phi_area=True, taper_s=0.05,
                 precision="split", device=device)
             pb = prepare_refracted(
                 pos, uct, b, [s], cfg.eps, cfg.att, mode="coherent", t0=t0,
                 dt=dt, n_samples=n_s, c=c, gamma=cfg.gamma_bed, k0=k0,
-                roughness=(rb["sigma"], rb["corr"], rb["phasors"], nt_b,
+                roughness=(rb["sigma"], rb["corr"], rb["phasors"], ntb,
                            "exponential"), d_phi_area=True, taper_s=0.05,
                 refraction="sequential", precision="split", device=device)
             return ps, pb
@@ -640,6 +640,32 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32):
                          "mufu_tops": mufu / (ms_k * 1e-3) / 1e12,
                          "mean_terms": [float(n_s_i.mean()),
                                         float(n_b_i.mean())]}}
+        # converged series: the parity runs keep the reference's 300-term
+        # cap (n_terms_for), which truncates D_Phi for the rough tail in the
+        # upper bands; the same runs with ceil(x + 6 sqrt(x) + 5) terms for
+        # the largest surface and 0.999-quantile bed x, where that fits the
+        # kernels' 4096-term limit
+        key = f"{f0 / 1e6:.0f}MHz"
+        try:
+            xs = (2 * k0 * rs["sigma"].max()) ** 2
+            xb = (2 * k0 * np.sqrt(3.15) *
+                  np.quantile(rb["sigma"], 0.999)) ** 2
+            cs, cb = (max(10, int(np.ceil(x + 6.0 * np.sqrt(x) + 5.0)))
+                      for x in (xs, xb))
+            if (cs, cb) == (nt_s, nt_b):
+                conv = {"n_terms": [cs, cb], "same_as_parity": True}
+            elif max(cs, cb) <= 4096:
+                cps, cpb = plans(cfg.pos, cfg.uct, cs, cb)
+                ms_c = _events_ms(lambda: (cps.run(), cpb.run()), 2, flush)
+                conv = {"n_terms": [cs, cb], "kernel_ms": ms_c,
+                        "contribs_per_s": pairs / (ms_c * 1e-3)}
+                del cps, cpb
+            else:
+                conv = {"n_terms": [cs, cb],
+                        "note": "above the kernels' 4096-term limit"}
+        except Exception as exc:  # reported, not hidden
+            conv = {"error": f"{type(exc).__name__}: {exc}"}
+        bands[key]["converged_series"] = conv
         # split form against the FP64 form on the central traces (both
         # targets' binned fields); a failure here is reported in the band
         if cfg3_error_traces:
