@@ -490,7 +490,28 @@ def _roof(flop, ms, peak, bound, per_unit, note):
             "flop_per_unit": per_unit, "ms": ms, "note": note}
 
 
-def row_cfg1(device, flush, peaks):
+def cfg1_cpu_baseline(cfg, seconds):
+    """The float64 NumPy oracle's coherent facet sum (the reference's
+    formulas) on one host core, over consecutive 8-trace slices of the
+    plain-surface track until about ``seconds`` have passed."""
+    from oracle import lpa
+    f = cfg.facets
+    T, N = len(cfg.pos), len(f.centers)
+    t0 = time.perf_counter()
+    done = 0
+    while done < T and time.perf_counter() - t0 < seconds:
+        sl = slice(done, min(done + 8, T))
+        lpa.coherent_cluttergram(cfg.pos[sl], cfg.uct[sl], f.centers,
+                                 f.normals, f.areas, f.e1, f.e2, **cfg.kw)
+        done = sl.stop
+    el = time.perf_counter() - t0
+    return {"value": done * N / el, "unit": "contribs/s", "cores": 1,
+            "kind": "port",
+            "sample": f"{done} traces x {N} facets, float64 NumPy oracle, "
+                      f"{el:.1f} s"}
+
+
+def row_cfg1(device, flush, peaks, cpu_seconds=0.0):
     """Plain surface, delta-binned coherent sum + LFM pulse compression."""
     from radar_sounder_simulator_gb300 import scenes
     from radar_sounder_simulator_gb300.coherent import prepare_coherent
@@ -530,7 +551,20 @@ def row_cfg1(device, flush, peaks):
                 "roofline": _roof(T * fft_flop, ms_rc, peaks["fp64"], "fp64",
                                   fft_flop, f"float64 FFT convolution per "
                                   f"row: 2 x 5 N log2 N + 6 N, N = {n_fft}")},
-            "error_vs_fp64": _errors(out["split"], out["fp64"])}
+            "error_vs_fp64": _errors(out["split"], out["fp64"]),
+            "cpu_baseline": _cpu_or_error(
+                lambda: cfg1_cpu_baseline(cfg, cpu_seconds), cpu_seconds)}
+
+
+def _cpu_or_error(fn, seconds):
+    """A row's CPU baseline, None when not asked for, the error text when
+    it fails (the row's GPU figures still stand)."""
+    if not seconds:
+        return None
+    try:
+        return fn()
+    except Exception as exc:  # reported, not hidden
+        return {"error": f"{type(exc).__name__}: {exc}"}
 
 
 def row_modef(device, flush, peaks):
@@ -1003,7 +1037,8 @@ def run_rows(args, device, peak32):
     rows["peaks_tflops"] = {**peaks, "source": "probes measured in this run "
                             "(ss_fp32_fma_probe, ss_fp64_fma_probe, "
                             "ss_mufu_probe)"}
-    fns = {"cfg1": lambda: row_cfg1(device, flush, peaks),
+    fns = {"cfg1": lambda: row_cfg1(device, flush, peaks,
+                                    min(args.cpu_seconds, 5.0)),
            "modef": lambda: row_modef(device, flush, peaks),
            "cfg3": lambda: row_cfg3(device, flush, peaks,
                                     0 if args.skip_fp64 else 32),

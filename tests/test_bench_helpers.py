@@ -55,3 +55,14 @@ def test_errors_ignore_bins_below_minus_60_db():
     e = bench._errors(a, b)
     assert e["phase_rad"] == 0.0 and e["power_db"] == 0.0
     assert e["rel_l2"] > 0.0
+
+
+def test_plain_surface_cpu_baseline_and_row_guard():
+    from radar_sounder_simulator_gb300 import scenes
+    cfg = scenes.config1()
+    cb = bench.cfg1_cpu_baseline(cfg, 0.01)      # one 8-trace slice
+    assert cb["value"] > 0 and cb["cores"] == 1 and cb["kind"] == "port"
+    assert cb["sample"].startswith("8 traces x 16384 facets")
+    assert bench._cpu_or_error(lambda: cb, 0.0) is None
+    err = bench._cpu_or_error(lambda: 1 / 0, 1.0)
+    assert err["error"].startswith("ZeroDivisionError")
