@@ -493,13 +493,14 @@ def _roof(flop, ms, peak, bound, per_unit, note):
 def cfg1_cpu_baseline(cfg, seconds):
     """The float64 NumPy oracle's coherent facet sum (the reference's
     formulas) on one host core, over consecutive 8-trace slices of the
-    plain-surface track until about ``seconds`` have passed."""
+    plain-surface track until about ``seconds`` have passed (at least one
+    slice)."""
     from oracle import lpa
     f = cfg.facets
     T, N = len(cfg.pos), len(f.centers)
     t0 = time.perf_counter()
     done = 0
-    while done < T and time.perf_counter() - t0 < seconds:
+    while done < T and (done == 0 or time.perf_counter() - t0 < seconds):
         sl = slice(done, min(done + 8, T))
         lpa.coherent_cluttergram(cfg.pos[sl], cfg.uct[sl], f.centers,
                                  f.normals, f.areas, f.e1, f.e2, **cfg.kw)
@@ -567,7 +568,31 @@ def _cpu_or_error(fn, seconds):
         return {"error": f"{type(exc).__name__}: {exc}"}
 
 
-def row_modef(device, flush, peaks):
+def modef_cpu_baseline(cfg, twtt, n_freq, seconds):
+    """The float64 NumPy oracle's frequency-sampled profile (the reference's
+    multifreq_profile steps) on one host core, position by position along
+    the plain-surface track until about ``seconds`` have passed (at least
+    one position)."""
+    from oracle import multifreq as omf
+    f = cfg.facets
+    t0 = time.perf_counter()
+    done = 0
+    while done < len(cfg.pos) and (done == 0 or
+                                   time.perf_counter() - t0 < seconds):
+        omf.multifreq_profile(cfg.pos[done], f.centers, f.normals, f.areas,
+                              f.e1, f.e2, gamma=cfg.kw["gamma"], f0=cfg.f0,
+                              bandwidth=cfg.bw, c=cfg.kw["c"], twtt=twtt,
+                              n_freq=n_freq, freeze_amplitudes=True)
+        done += 1
+    el = time.perf_counter() - t0
+    return {"value": done * len(f.centers) * n_freq / el,
+            "unit": "pair-frequencies/s", "cores": 1, "kind": "port",
+            "sample": f"{done} positions x {len(f.centers)} facets x "
+                      f"{n_freq} frequencies, float64 NumPy oracle, "
+                      f"{el:.1f} s"}
+
+
+def row_modef(device, flush, peaks, cpu_seconds=0.0):
     """Frequency-sampled synthesis of the config-1 scene, K = 1024."""
     from radar_sounder_simulator_gb300 import scenes
     from radar_sounder_simulator_gb300.multifreq import prepare_multifreq
@@ -595,7 +620,10 @@ def row_modef(device, flush, peaks):
                               8.0, "band response (main pass + reduce), 8 "
                               "FLOP per pair-frequency (complex rotate and "
                               "accumulate, frozen amplitudes)"),
-            "error_vs_fp64": _errors(res["split"], res["fp64"])}
+            "error_vs_fp64": _errors(res["split"], res["fp64"]),
+            "cpu_baseline": _cpu_or_error(
+                lambda: modef_cpu_baseline(cfg, tw, 1024, cpu_seconds),
+                cpu_seconds)}
 
 
 def row_cfg3(device, flush, peaks, cfg3_error_traces=32):
@@ -1039,7 +1067,8 @@ def run_rows(args, device, peak32):
                             "ss_mufu_probe)"}
     fns = {"cfg1": lambda: row_cfg1(device, flush, peaks,
                                     min(args.cpu_seconds, 5.0)),
-           "modef": lambda: row_modef(device, flush, peaks),
+           "modef": lambda: row_modef(device, flush, peaks,
+                                      min(args.cpu_seconds, 5.0)),
            "cfg3": lambda: row_cfg3(device, flush, peaks,
                                     0 if args.skip_fp64 else 32),
            "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,

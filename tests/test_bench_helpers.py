@@ -66,3 +66,12 @@ def test_plain_surface_cpu_baseline_and_row_guard():
     assert bench._cpu_or_error(lambda: cb, 0.0) is None
     err = bench._cpu_or_error(lambda: 1 / 0, 1.0)
     assert err["error"].startswith("ZeroDivisionError")
+
+
+def test_mode_f_cpu_baseline_one_position():
+    from radar_sounder_simulator_gb300 import scenes
+    cfg = scenes.config1()
+    tw = cfg.kw["t0"] + np.arange(64) * cfg.kw["dt"]
+    cb = bench.modef_cpu_baseline(cfg, tw, 64, 1e-6)   # one position
+    assert cb["value"] > 0 and cb["unit"] == "pair-frequencies/s"
+    assert cb["sample"].startswith("1 positions x 16384 facets x 64")
