@@ -72,6 +72,7 @@ def test_mode_f_cpu_baseline_one_position():
     from radar_sounder_simulator_gb300 import scenes
     cfg = scenes.config1()
     tw = cfg.kw["t0"] + np.arange(64) * cfg.kw["dt"]
-    cb = bench.modef_cpu_baseline(cfg, tw, 64, 1e-6)   # one position
+    # K = 1024 keeps the referee's alias guard satisfied (K/B > delay span)
+    cb = bench.modef_cpu_baseline(cfg, tw, 1024, 1e-6)   # one position
     assert cb["value"] > 0 and cb["unit"] == "pair-frequencies/s"
-    assert cb["sample"].startswith("1 positions x 16384 facets x 64")
+    assert cb["sample"].startswith("1 positions x 16384 facets x 1024")
