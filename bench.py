@@ -626,7 +626,45 @@ def row_modef(device, flush, peaks, cpu_seconds=0.0):
                 cpu_seconds)}
 
 
-def row_cfg3(device, flush, peaks, cfg3_error_traces=32):
+def cfg3_cpu_baseline(cfg, band, seconds):
+    """The float64 NumPy oracle on one host core for one band of the
+    roughness configuration -- the rough surface's coherent sum and the
+    rough bed refracted through it -- trace by trace from the middle of the
+    track until about ``seconds`` have passed (at least one trace)."""
+    from oracle import lpa
+    from oracle import refracted as oref
+    s, b = cfg.surface, cfg.bed
+    rs, rb = cfg.rough["surface"], cfg.rough["bed"]
+    common = dict(t0=band["t0"], dt=band["dt"], n_samples=band["n_s"],
+                  c=cfg.c, d_phi_area=True, taper_s=0.05)
+    T = len(cfg.pos)
+    mid = T // 2
+    t0 = time.perf_counter()
+    done = 0
+    while mid + done < T and (done == 0 or
+                              time.perf_counter() - t0 < seconds):
+        sl = slice(mid + done, mid + done + 1)
+        lpa.coherent_cluttergram(
+            cfg.pos[sl], cfg.uct[sl], s.centers, s.normals, s.areas, s.e1,
+            s.e2, k=band["k0"], gamma=cfg.gamma_surface,
+            roughness=(rs["sigma"], rs["corr"], rs["phasors"], band["nt_s"],
+                       "exponential"), **common)
+        oref.refracted_cluttergram(
+            cfg.pos[sl], cfg.uct[sl], b, [s], cfg.eps, cfg.att,
+            mode="coherent", gamma=cfg.gamma_bed, k0=band["k0"],
+            roughness=(rb["sigma"], rb["corr"], rb["phasors"], band["nt_b"],
+                       "exponential"), refraction="sequential", **common)
+        done += 1
+    el = time.perf_counter() - t0
+    n = len(s.centers) + len(b.centers)
+    return {"value": done * n / el, "unit": "contribs/s", "cores": 1,
+            "kind": "port",
+            "sample": f"{done} traces x {n} facets (surface + bed) at "
+                      f"{band['k0'] * cfg.c / (2 * np.pi) / 1e6:.0f} MHz, "
+                      f"float64 NumPy oracle, {el:.1f} s"}
+
+
+def row_cfg3(device, flush, peaks, cfg3_error_traces=32, cpu_seconds=0.0):
     """Rough surface and bed, four bands: per band the surface coherent sum
     and the refracted bed sum (per-facet sigma, l; exponential ACF with the
     area-only series and taper), each pulse-compressed."""
@@ -728,6 +766,11 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32):
         except Exception as exc:  # reported, not hidden
             conv = {"error": f"{type(exc).__name__}: {exc}"}
         bands[key]["converged_series"] = conv
+        if f0 == 60e6:
+            bands[key]["cpu_baseline"] = _cpu_or_error(
+                lambda: cfg3_cpu_baseline(
+                    cfg, dict(k0=k0, t0=t0, dt=dt, n_s=n_s, nt_s=nt_s,
+                              nt_b=nt_b), cpu_seconds), cpu_seconds)
         # split form against the FP64 form on the central traces (both
         # targets' binned fields); a failure here is reported in the band
         if cfg3_error_traces:
@@ -1070,7 +1113,8 @@ def run_rows(args, device, peak32):
            "modef": lambda: row_modef(device, flush, peaks,
                                       min(args.cpu_seconds, 5.0)),
            "cfg3": lambda: row_cfg3(device, flush, peaks,
-                                    0 if args.skip_fp64 else 32),
+                                    0 if args.skip_fp64 else 32,
+                                    min(args.cpu_seconds, 5.0)),
            "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,
                                     peaks),
            "cfg5": lambda: row_cfg5(device, flush),

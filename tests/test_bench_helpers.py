@@ -76,3 +76,18 @@ def test_mode_f_cpu_baseline_one_position():
     cb = bench.modef_cpu_baseline(cfg, tw, 1024, 1e-6)   # one position
     assert cb["value"] > 0 and cb["unit"] == "pair-frequencies/s"
     assert cb["sample"].startswith("1 positions x 16384 facets x 1024")
+
+
+def test_roughness_cpu_baseline_one_trace():
+    from radar_sounder_simulator_gb300 import scenes
+    cfg = scenes.config3(n_cells=32, n_traces=8)
+    f0 = 60e6
+    dt = 1.0 / (2.0 * cfg.frac_bw * f0)
+    k0 = 2 * np.pi * f0 / cfg.c
+    n_s = 256
+    t0 = scenes.window(cfg.pos, cfg.surface.centers, n_samples=n_s, dt=dt)
+    band = dict(k0=k0, t0=t0, dt=dt, n_s=n_s, nt_s=15, nt_b=60)
+    cb = bench.cfg3_cpu_baseline(cfg, band, 0.0)     # one trace
+    assert cb["value"] > 0 and cb["unit"] == "contribs/s"
+    assert cb["sample"].startswith("1 traces x 2048 facets (surface + bed) "
+                                   "at 60 MHz")
