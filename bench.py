@@ -802,7 +802,39 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32, cpu_seconds=0.0):
                              "the FMA and MUFU rates measured in this run"}
 
 
-def row_cfg4(device, n_inst, flush, peaks):
+def cfg4_cpu_baseline(seconds):
+    """The float64 NumPy oracle on one host core for the sweep's first
+    instance (tabulated antenna pattern): 8-trace slices from the middle of
+    its track, every facet of every trace (no culling), until about
+    ``seconds`` have passed (at least one slice)."""
+    from oracle import lpa
+    from radar_sounder_simulator_gb300 import scenes
+    inst = scenes.config4_instance(0)
+    f = inst.facets
+    T, N = len(inst.pos), len(f.centers)
+    kind, pv, pa, pb = inst.kw["pattern"]
+    pv = np.asarray(pv, np.float64).reshape(T, -1)
+    kw = {k: v for k, v in inst.kw.items() if k != "pattern"}
+    mid = T // 2
+    t0 = time.perf_counter()
+    done = 0
+    while mid + done < T and (done == 0 or
+                              time.perf_counter() - t0 < seconds):
+        sl = slice(mid + done, min(mid + done + 8, T))
+        lpa.coherent_cluttergram(inst.pos[sl], inst.uct[sl], f.centers,
+                                 f.normals, f.areas, f.e1, f.e2,
+                                 pattern=(kind, pv[sl], pa, pb),
+                                 window_cull=False, **kw)
+        done = sl.stop - mid
+    el = time.perf_counter() - t0
+    return {"value": done * N / el, "unit": "contribs/s", "cores": 1,
+            "kind": "port",
+            "sample": f"{done} traces x {N} facets of instance 0 (every "
+                      f"pair, tabulated pattern), float64 NumPy oracle, "
+                      f"{el:.1f} s"}
+
+
+def row_cfg4(device, n_inst, flush, peaks, cpu_seconds=0.0):
     """Batched design sweep: one persistent work-queue launch over all
     instances, captured in a CUDA graph, autotuned decomposition."""
     import torch
@@ -861,7 +893,9 @@ def row_cfg4(device, n_inst, flush, peaks):
                             "split_ms": ms_sub, "fp64_ms": ms64,
                             "split_over_fp64": ms64 / ms_sub,
                             "window_pairs": sub_pairs},
-            "error_vs_fp64": err}
+            "error_vs_fp64": err,
+            "cpu_baseline": _cpu_or_error(
+                lambda: cfg4_cpu_baseline(cpu_seconds), cpu_seconds)}
 
 
 def row_cfg5(device, flush):
@@ -1116,7 +1150,7 @@ def run_rows(args, device, peak32):
                                     0 if args.skip_fp64 else 32,
                                     min(args.cpu_seconds, 5.0)),
            "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,
-                                    peaks),
+                                    peaks, min(args.cpu_seconds, 5.0)),
            "cfg5": lambda: row_cfg5(device, flush),
            "incoh": lambda: row_incoh(device, flush, peaks),
            "focus": lambda: row_focus(device, flush, peaks),

@@ -91,3 +91,9 @@ def test_roughness_cpu_baseline_one_trace():
     assert cb["value"] > 0 and cb["unit"] == "contribs/s"
     assert cb["sample"].startswith("1 traces x 2048 facets (surface + bed) "
                                    "at 60 MHz")
+
+
+def test_sweep_cpu_baseline_one_slice():
+    cb = bench.cfg4_cpu_baseline(0.0)                  # one 8-trace slice
+    assert cb["value"] > 0 and cb["unit"] == "contribs/s"
+    assert cb["sample"].startswith("8 traces x ")
