@@ -39,7 +39,12 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-cells", type=int, default=512)
     ap.add_argument("--n-traces", type=int, default=1024)
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="host time of the headline's CPU baseline; the "
+                         "one-core baselines of the plain-surface, Mode F, "
+                         "roughness and sweep rows take at most 5 s each "
+                         "and 0 skips them (the smaller rows time a fixed "
+                         "small sample)")
     ap.add_argument("--skip-fp64", action="store_true",
                     help="skip the float64-form step and the error check")
     ap.add_argument("--skip-e2e", action="store_true",
