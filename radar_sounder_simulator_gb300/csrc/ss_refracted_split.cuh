@@ -27,8 +27,11 @@
 //     error enters at second order; the crossing's float32 offset from the
 //     facet plane (up to ~1e-5 m for far crossings) enters at first order,
 //     and the sequential path adds it back (height from exact products
-//     times the legs' index-weighted cosines). A pair whose bin position
-//     lies within 5e-5 m of optical path (at
+//     times the legs' index-weighted cosines). A sequential chain through
+//     two or more interfaces is not stationary in its upper crossings, so
+//     their float32 in-plane error also enters at first order (~1e-5 m,
+//     rarely ~1e-4 m). A pair whose bin position
+//     lies within 5e-5 m of optical path (2e-4 m for such chains; at
 //     least 1e-6 bins) of a bin edge is re-evaluated with the complete
 //     float64 path, so bins equal the float64 form's also for the fine bins
 //     of the high bands;
