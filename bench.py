@@ -224,58 +224,63 @@ class ClockSampler:
 
 
 # --------------------------------------------------------------------------
-# CPU baseline / reference arm (float64 oracle restatement on host cores)
+# CPU baseline / reference arm: the reference formulas restated in C++17
+# (float64, OpenMP over traces, every host core), test infrastructure under
+# oracle/ and pinned there to the NumPy oracle and the reference fixtures
 # --------------------------------------------------------------------------
-def _oracle_sample(args_tuple):
-    """Worker: one trace of one layer through the NumPy float64 oracle."""
-    (layer, j, pos, uct, cfg_small) = args_tuple
-    from oracle import lpa, refracted
-    if j == 0:
-        f = layer[0]
-        out, _ = lpa.coherent_cluttergram(
-            pos, uct, f.centers, f.normals, f.areas, f.e1, f.e2,
-            k=cfg_small["k0"], gamma=cfg_small["gammas"][0],
-            t0=cfg_small["t0"], dt=cfg_small["dt"],
-            n_samples=cfg_small["n_samples"], c=cfg_small["c"])
-    else:
-        refr = "joint" if j > 1 else "sequential"
-        out, _ = refracted.refracted_cluttergram(
-            pos, uct, layer[j], layer[:j], cfg_small["eps"][:j + 1],
-            cfg_small["att"][:j + 1], mode="coherent", t0=cfg_small["t0"],
-            dt=cfg_small["dt"], n_samples=cfg_small["n_samples"],
-            c=cfg_small["c"], gamma=cfg_small["gammas"][j],
-            k0=cfg_small["k0"], refraction=refr)
-    return len(layer[j].centers) * len(pos)
+CPU_KIND_NOTE = ("reference formulas, host restatement: C++17 OpenMP "
+                 "float64 (oracle/cpu_ref.cpp), the reference's JAX CPU "
+                 "path being unavailable (jax is not installed)")
 
 
-def cpu_sample_rate(cfg, seconds, cores):
-    """Oracle pairs/s on a bounded sample: whole layers, a few traces, spread
-    over ``cores`` spawned worker processes; grows the sample until it takes
-    about ``seconds``."""
-    import multiprocessing as mp
-    small = dict(k0=cfg.k0, gammas=cfg.gammas, t0=cfg.t0, dt=cfg.dt,
-                 n_samples=cfg.n_samples, c=cfg.c, eps=cfg.eps, att=cfg.att)
-    ctx = mp.get_context("spawn")
+def cpu_batch(cfg, sel):
+    """One sample batch: the traces ``sel`` through all four targets of the
+    multilayer scene on the host restatement. Returns the pairs done."""
+    from oracle import cpu_ref
+    L = cfg.layers
+    pairs = 0
+    for j in range(4):
+        if j == 0:
+            f = L[0]
+            cpu_ref.coherent_cluttergram(
+                cfg.pos[sel], cfg.uct[sel], f.centers, f.normals, f.areas,
+                f.e1, f.e2, k=cfg.k0, gamma=cfg.gammas[0], t0=cfg.t0,
+                dt=cfg.dt, n_samples=cfg.n_samples, c=cfg.c)
+        else:
+            cpu_ref.refracted_cluttergram(
+                cfg.pos[sel], cfg.uct[sel], L[j], L[:j], cfg.eps[:j + 1],
+                cfg.att[:j + 1], mode="coherent", t0=cfg.t0, dt=cfg.dt,
+                n_samples=cfg.n_samples, c=cfg.c, gamma=cfg.gammas[j],
+                k0=cfg.k0, refraction=cfg.refraction if j > 1
+                else "sequential")
+        pairs += len(L[j].centers) * len(sel)
+    return pairs
+
+
+def cpu_sample_rate(cfg, seconds, start=0):
+    """Host restatement pairs/s on a bounded sample of the benchmark
+    workload: batches of seeded trace picks (one trace per thread at
+    least), each through all four whole targets, until about ``seconds``
+    have passed (at least one batch). Returns (rate, sample text, threads,
+    seconds, next start)."""
+    from oracle import cpu_ref
+    cpu_ref.build()
+    th = cpu_ref.threads()
     T = len(cfg.pos)
-    jobs = []
-    rng = np.random.default_rng(0)
-    picks = rng.choice(T, size=min(T, 4 * cores), replace=False)
-    for t in picks:
-        for j in range(4):
-            jobs.append((cfg.layers, j, cfg.pos[t:t + 1], cfg.uct[t:t + 1],
-                         small))
-    with ctx.Pool(cores) as pool:
-        t0 = time.perf_counter()
-        done = 0
-        it = pool.imap_unordered(_oracle_sample, jobs)
-        for n in it:
-            done += n
-            if time.perf_counter() - t0 > seconds:
-                pool.terminate()
-                break
-        el = time.perf_counter() - t0
-    return done / el, f"{done} pairs ({len(picks)} traces x 4 layers max, " \
-                      f"whole layers) in {el:.1f} s"
+    picks = np.random.default_rng(0).permutation(T)
+    per = max(th, 8)
+    t0 = time.perf_counter()
+    done = n_tr = 0
+    k = start
+    while done == 0 or time.perf_counter() - t0 < seconds:
+        lo = (k * per) % T
+        sel = np.sort(picks[lo:lo + per])
+        done += cpu_batch(cfg, sel)
+        n_tr += len(sel)
+        k += 1
+    el = time.perf_counter() - t0
+    return (done / el, f"{done} pairs ({n_tr} traces x 4 whole targets) "
+                       f"in {el:.1f} s on {th} threads", th, el, k)
 
 
 def run_reference(args):
@@ -284,28 +289,32 @@ def run_reference(args):
         return
     from radar_sounder_simulator_gb300 import scenes
     cfg = scenes.config2(n_cells=args.n_cells, n_traces=args.n_traces)
-    cores = os.cpu_count() or 1
-    vals = []
+    per_step = max(args.cpu_seconds / 4.0, 0.5)
+    k = 0
     for _ in range(args.warmup):
-        cpu_sample_rate(cfg, min(args.cpu_seconds, 5.0), cores)
+        _, _, _, _, k = cpu_sample_rate(cfg, 0.0, k)
+    rates, secs, pairs = [], [], 0
+    th, sample = 1, ""
     for _ in range(args.steps):
-        v, sample = cpu_sample_rate(cfg, args.cpu_seconds / 2, cores)
-        vals.append(v)
-    value = float(np.median(vals))
-    pairs_step = 4 * args.n_cells ** 2 * args.n_traces
+        v, sample, th, el, k = cpu_sample_rate(cfg, per_step, k)
+        rates.append(v)
+        secs.append(el)
+        pairs += v * el
+    value = pairs / sum(secs)
     line = {"impl": "reference", "metric": METRIC, "value": value,
             "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": pairs_step / value * 1e3,
+            "warmup": args.warmup,
+            "ms_per_step": float(np.mean(secs)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64", "data": "synthetic (seeded config-2 scene)",
             "config": config_dict(args, ws),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": th,
                              "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "reference JAX CPU path unavailable on this host (jax "
-                    "not installed); float64 NumPy restatement of the "
-                    "reference formulas timed instead"}
+            "note": "each step is a bounded sample of the workload (one "
+                    "batch of traces through all four whole targets); "
+                    "ms_per_step is that sample's time. " + CPU_KIND_NOTE}
     print(json.dumps(line), flush=True)
 
 
@@ -421,10 +430,9 @@ def main():
     if rank == 0:
         cpu = None
         if ws == 1 and args.cpu_seconds > 0:
-            v, sample = cpu_sample_rate(cfg, args.cpu_seconds,
-                                        os.cpu_count() or 1)
-            cpu = {"value": v, "unit": UNIT, "cores": os.cpu_count() or 1,
-                   "kind": "port", "sample": sample}
+            v, sample, th, _, _ = cpu_sample_rate(cfg, args.cpu_seconds)
+            cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
+                   "sample": sample, "note": CPU_KIND_NOTE}
         rows = run_rows(args, device, peak) if ws == 1 else None
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws,
                 "steps": args.steps, "warmup": args.warmup,
