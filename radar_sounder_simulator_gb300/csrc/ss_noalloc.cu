@@ -63,37 +63,18 @@ extern "C" int ss_coherent_fwd_noalloc(const ss_coherent_opts *opts,
                                        const ss_roughness *rough,
                                        const ss_output *out, void *stream) {
   using namespace ss;
-  if (!opts || !facets || !traces || !out) {
-    set_error("null argument");
-    return SS_ERR_ARG;
-  }
-  const int T = traces->n_traces, N = facets->n_facets;
-  if (!traces->pos || !traces->off || !facets->cx || !facets->area ||
-      !out->dropped || (!out->field_c128 && !out->field_c64)) {
-    set_error("missing required device pointer");
-    return SS_ERR_ARG;
-  }
-  if (opts->split_sides && !traces->uct) {
-    set_error("split_sides needs u_ct");
-    return SS_ERR_ARG;
-  }
-  if (opts->precision != SS_PREC_FP64 && opts->precision != SS_PREC_SPLIT) {
-    set_error("unknown precision");
-    return SS_ERR_ARG;
-  }
+  // the same validation and argument block as ss_coherent_fwd
   Plan p;
-  int s = coherent_plan(opts, T, N, &p);
-  if (s) {
-    set_error(s == SS_ERR_UNSUPPORTED ? "n_samples too large for the "
-                                        "shared-memory histogram"
-                                      : "bad sizes");
-    return s;
-  }
+  CoArgs a;
+  int s = build_co_args(opts, facets, traces, pattern, rough, out, p, a);
+  if (s) return s;
+  const int T = traces->n_traces;
   // As many facet chunks as the fixed array holds (at most what
-  // ss_coherent_fwd would use); one chunk must fit.
-  const int n_seg = opts->n_samples * (opts->split_sides ? 2 : 1);
+  // ss_coherent_fwd would use); one chunk must fit. coherent_launch takes
+  // the chunk count from the plan, and every partial the reduction reads
+  // is written by the main kernel first.
   const size_t elt = opts->precision == SS_PREC_FP64 ? 16 : 8;
-  const size_t hist1 = (size_t)T * n_seg * elt;
+  const size_t hist1 = (size_t)T * a.n_seg * elt;
   auto need = [&](int nc) {
     size_t h = ((size_t)nc * hist1 + 255) & ~(size_t)255;
     return h + (size_t)nc * T * sizeof(double);
@@ -108,55 +89,6 @@ extern "C" int ss_coherent_fwd_noalloc(const ss_coherent_opts *opts,
   void *scratch = nullptr;
   s = noalloc_scratch(&scratch);
   if (s) return s;
-
-  CoArgs a{};
-  a.F = *facets;
-  a.pos = traces->pos;
-  a.uct = traces->uct;
-  a.pv = traces->pv;
-  a.off = traces->off;
-  a.T = T;
-  a.N = N;
-  a.pv_len = traces->pv_len;
-  a.k = opts->k;
-  a.gamma = opts->gamma;
-  a.t0 = opts->t0;
-  a.dt = opts->dt;
-  a.c = opts->c;
-  a.taper_s = opts->taper_s;
-  a.n_samples = opts->n_samples;
-  a.n_seg = n_seg;
-  a.bs = opts->block_size;
-  a.n_win = opts->n_win;
-  a.split = opts->split_sides;
-  a.interp = opts->interp_bins;
-  a.taper = opts->taper;
-  a.precision = opts->precision;
-  a.pat_kind = pattern ? pattern->kind : SS_PAT_ISOTROPIC;
-  a.pat_n = pattern ? pattern->n : 0;
-  a.pa = pattern ? pattern->pa : nullptr;
-  a.pb = pattern ? pattern->pb : nullptr;
-  if (a.pat_kind != SS_PAT_ISOTROPIC && (!traces->pv || traces->pv_len < 3)) {
-    set_error("antenna pattern needs per-trace pattern vectors");
-    return SS_ERR_ARG;
-  }
-  if ((a.pat_kind == SS_PAT_ARRAY || a.pat_kind == SS_PAT_ARRAY_TAPERED) &&
-      traces->pv_len < 6) {
-    set_error("array patterns need (T, 2, 3) pattern vectors");
-    return SS_ERR_ARG;
-  }
-  a.rough_kind = rough ? rough->kind : SS_ROUGH_NONE;
-  if (a.rough_kind != SS_ROUGH_NONE) {
-    if (!facets->phasor || rough->n_terms < 0 ||
-        rough->n_terms > SS_MAX_TERMS) {
-      set_error("roughness needs phasors and 0 <= n_terms <= 4096");
-      return SS_ERR_ARG;
-    }
-    a.n_terms = rough->n_terms;
-    a.sigma = rough->sigma;
-    a.corr = rough->corr;
-    a.fad = faddeeva_coeffs();
-  }
   a.part = scratch;
   const size_t hist = ((size_t)p.n_chunks * hist1 + 255) & ~(size_t)255;
   a.part_drop = reinterpret_cast<double *>(static_cast<char *>(scratch) +
