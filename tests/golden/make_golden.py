@@ -1,6 +1,8 @@
 """Freeze the reference's own outputs as golden fixtures (run here, once).
 
-    PYTHONPATH=. python tests/golden/make_golden.py [--only a,b] [/path/to/reference]
+    SOUNDERSIM_REF=/path/to/reference PYTHONPATH=. \
+        python tests/golden/make_golden.py [--only a,b]
+    PYTHONPATH=. python tests/golden/make_golden.py [--only a,b] /path/to/reference
 
 Runs the UNMODIFIED soundersim source (``refload`` + ``jaxshim``: NumPy in
 place of JAX) on small seeded scenes and writes ``tests/golden/*.npz``.
@@ -536,8 +538,6 @@ def main():
         args = args[2:]
     if args:
         os.environ["SOUNDERSIM_REF"] = args[0]
-        refload.REF_ROOT = args[0]
-        refload.SRC = os.path.join(args[0], "src", "soundersim")
     ns = refload.load()
     for name, fn in (("primitives", make_primitives), ("antenna", make_antenna),
                      ("coherent", make_coherent),

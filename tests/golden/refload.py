@@ -15,12 +15,20 @@ import types
 
 from . import jaxshim
 
-REF_ROOT = os.environ.get("SOUNDERSIM_REF", "/root/reference")
-SRC = os.path.join(REF_ROOT, "src", "soundersim")
+def _src():
+    """The reference's ``src/soundersim`` directory, from the checkout named
+    by the ``SOUNDERSIM_REF`` environment variable (required: there is no
+    default location)."""
+    root = os.environ.get("SOUNDERSIM_REF")
+    if not root:
+        raise RuntimeError("set SOUNDERSIM_REF to the soundersim checkout "
+                           "(the directory holding src/soundersim)")
+    return os.path.join(root, "src", "soundersim")
 
 
 def load():
     """Return a namespace with the reference modules used by the fixtures."""
+    SRC = _src()
     jaxshim.install()
     for name, sub in (("soundersim", ""), ("soundersim.kernels", "kernels"),
                       ("soundersim.compare", "compare")):
