@@ -257,7 +257,7 @@ namespace ss {
 
 // Validate the call and fill the argument block shared by the forward and
 // adjoint entry points (everything but the scratch layout).
-static int build_ref_args(const ss_refracted_opts *opts,
+int build_ref_args(const ss_refracted_opts *opts,
                           const ss_facets *target, const ss_traces *traces,
                           const ss_pattern *pattern, const ss_roughness *rough,
                           bool need_output, const ss_output *out, Plan &p,

@@ -38,6 +38,13 @@ constexpr int kSplitThreads = 512;
 
 int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st);
 
+// Validate one refracted call and fill its argument block (everything but
+// the scratch layout); shared by the forward and adjoint entry points.
+int build_ref_args(const ss_refracted_opts *opts, const ss_facets *target,
+                   const ss_traces *traces, const ss_pattern *pattern,
+                   const ss_roughness *rough, bool need_output,
+                   const ss_output *out, Plan &p, RefArgs &a);
+
 // Adjoint inputs and outputs (see ss_refracted_adjoint).
 struct AdjArgs {
   const double *field;       // (T, n_seg, 2) forward field

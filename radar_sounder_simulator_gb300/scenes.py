@@ -168,9 +168,13 @@ def n_terms_for(x_max):
     return int(np.clip(np.ceil(x + 6.0 * np.sqrt(x) + 5.0), 10, 300))
 
 
-def speckle_phasors(n, rng):
-    """Unit-variance complex Gaussian speckle phasors (roughness.py:199-204
-    form), complex64."""
+def speckle_phasors(n, seed):
+    """Unit-variance complex Gaussian speckle phasors, complex64, drawn the
+    way the reference's ``speckle_phasors(n, seed)`` draws them
+    (roughness.py:199-204: a fresh ``default_rng(seed)``, real parts then
+    imaginary parts), so a keyed seed such as ``(scene_seed, layer)`` gives
+    the reference's own phasors bit for bit."""
+    rng = np.random.default_rng(seed)
     ph = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     return (ph / np.sqrt(2.0)).astype(np.complex64)
 
@@ -194,16 +198,37 @@ def config3(seed=3, n_cells=512, n_traces=2048, spacing=25.0,
     rough = dict(
         surface=dict(sigma=rng.uniform(0.05, 0.5, n),
                      corr=rng.uniform(5.0, 50.0, n),
-                     phasors=speckle_phasors(n, rng)),
+                     phasors=speckle_phasors(n, (seed, 0))),
         bed=dict(sigma=np.exp(np.log(0.3) + 0.7 * rng.standard_normal(n)),
                  corr=rng.uniform(5.0, 50.0, n),
-                 phasors=speckle_phasors(n, rng)))
+                 phasors=speckle_phasors(n, (seed, 1))))
     bands = [30e6, 60e6, 150e6, 450e6]
     return SimpleNamespace(surface=surf, bed=bed, pos=pos, uct=uct, eps=eps,
                            att=[0.0, 10.0], rough=rough, bands=bands,
                            frac_bw=0.10, n_freq=1024, c=C_LIGHT,
                            gamma_surface=fresnel_normal(1.0, 3.15),
                            gamma_bed=fresnel_normal(3.15, 9.0))
+
+
+def config3_band(cfg, f0):
+    """Fast-time window and series lengths of one band of the roughness
+    configuration: dt = 1/(2 B) for the 10% bandwidth, n_samples covering
+    the surface and the bed under 1000 m of ice plus 3 km of slant, t0 from
+    the surface's nearest range, and the reference's D_Phi series lengths
+    (n_terms_for) for the largest surface rms height and the 0.999 quantile
+    of the bed's (in ice). Returns a dict (f0, bw, k0, dt, n_s, t0, nt_s,
+    nt_b)."""
+    bw = cfg.frac_bw * f0
+    dt = 1.0 / (2.0 * bw)
+    k0 = 2 * np.pi * f0 / cfg.c
+    n_s = int(np.ceil(2 * (1000.0 * np.sqrt(3.15) + 3000.0) / cfg.c / dt))
+    t0 = window(cfg.pos, cfg.surface.centers, n_samples=n_s, dt=dt)
+    rs, rb = cfg.rough["surface"], cfg.rough["bed"]
+    nt_s = n_terms_for((2 * k0 * rs["sigma"].max()) ** 2)
+    nt_b = n_terms_for((2 * k0 * np.sqrt(cfg.eps[1]) *
+                        np.quantile(rb["sigma"], 0.999)) ** 2)
+    return dict(f0=f0, bw=bw, k0=k0, dt=dt, n_s=n_s, t0=t0, nt_s=nt_s,
+                nt_b=nt_b)
 
 
 def gaussian_beam_table(beamwidth_deg, n=64):
@@ -268,7 +293,7 @@ def config5(seed=5, n_cells=512, n_traces=1024, spacing=25.0,
                            eps=[1.0, 3.15], alpha=10.0, k0=2 * np.pi * f0 /
                            C_LIGHT, t0=t0, dt=dt, n_samples=1024, c=C_LIGHT,
                            R=R, sig=sig, R_hat=R_hat, sig_hat=sig_hat, window=(0, 1024),
-                           corr=10.0, phasors=speckle_phasors(n, rng),
+                           corr=10.0, phasors=speckle_phasors(n, (seed, 1)),
                            n_terms=n_terms)
 
 
