@@ -194,39 +194,53 @@ __device__ __forceinline__ void d_phi_range(float x, int n_terms, int &m_lo,
                                    : n_terms;
 }
 
-// D_Phi in float32; lg[m] = lgamma(m + 1).
+// Poisson weight P_m(x) = e^-x x^m / m! in float32 to a few ulp, for the
+// anchor of a run of terms. The direct form m ln x - ln m! - x cancels
+// terms of several hundred (1e-4 absolute at float32 rounding, i.e. 1e-4
+// relative in P near the 300-term cap), so for m >= 10 the anchor uses
+// Stirling's series for ln m! (Abramowitz & Stegun 6.1.41):
+//   ln P_m = m (log1p(-u) + u) - ln(2 pi m) / 2 - 1/(12 m) + 1/(360 m^3),
+// u = (m - x) / m, whose terms are small; the omitted 1/(1260 m^5) is
+// below 1e-8 at m = 10. Below m = 10, e^-x x^m / m! by products.
+__device__ __forceinline__ float poisson_anchor(int m, float x) {
+  const float mf = (float)m;
+  if (m < 10) {
+    float p = expf(-x);
+    for (int j = 1; j <= m; ++j) p *= x / (float)j;
+    return p;
+  }
+  const float u = (mf - x) / mf;
+  const float im = 1.0f / mf;
+  const float lp = mf * (log1pf(-u) + u) -
+                   0.5f * logf(6.28318530718f * mf) -
+                   im * (0.0833333333f - 0.00277777778f * im * im);
+  return expf(lp);
+}
+
+// D_Phi in float32. Poisson weights are exact (poisson_anchor) at the start
+// of every run of 64 terms and follow the recursion P_m = P_(m-1) x / m
+// inside it (a few roundings per step, ~1e-6 relative at a run's end).
 template <int KIND>
 __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
                                          const float *fa, float fL,
                                          float sigma, float l, float K,
                                          float A0, float B0, float Lx,
                                          float Ly) {
+  (void)lg;
   const float sk = sigma * K;
   const float x = sk * sk;
   if (!(x > 0.0f)) return 0.0f;
-  const float logx = __logf(x);
   const float kb2 = A0 * A0 + B0 * B0;
   int m_lo, m_hi;
   d_phi_range<KIND>(x, n_terms, m_lo, m_hi);
   float acc = 0.0f;
-  if (KIND == SS_ROUGH_GAUSS_AREA) {
-    const float c = 0.25f * kb2 * l * l;
-    const float pref = 3.14159265359f * l * l * Lx * Ly;
-    for (int m = m_lo; m <= m_hi; ++m) {
-      const float mf = (float)m;
-      const float im = __fdividef(1.0f, mf);
-      const float e = __fmaf_rn(mf, logx, -lg[m]) - x - c * im;
-      acc = __fmaf_rn(__expf(e), pref * im, acc);
-    }
-  } else if (KIND == SS_ROUGH_EXP_AREA) {
-    // Poisson weights exact at the start of every run of 64 terms and by
-    // the recursion P_m = P_(m-1) x / m inside it (a few roundings per
-    // step, ~1e-5 relative at a run's end); the prefactor leaves the loop.
-    // Per term: one reciprocal and one reciprocal square root.
+  if (KIND == SS_ROUGH_EXP_AREA) {
+    // W_m = 2 pi l^2 m^-2 (1 + (k_B l / m)^2)^(-3/2) Lx Ly: one reciprocal
+    // and one reciprocal square root per term, the prefactor outside
     const float kl2 = kb2 * l * l;
     for (int m0 = m_lo; m0 <= m_hi; m0 += 64) {
       float mf = (float)m0;
-      float P = __expf(__fmaf_rn(mf, logx, -lg[m0]) - x);
+      float P = poisson_anchor(m0, x);
       float im = __fdividef(1.0f, mf);
       float im2 = im * im;
       float rs = rsqrtf(__fmaf_rn(kl2, im2, 1.0f));
@@ -242,15 +256,32 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
       }
     }
     acc *= 6.28318530718f * l * l * Lx * Ly;
+  } else if (KIND == SS_ROUGH_GAUSS_AREA) {
+    // W_m = pi l^2 / m exp(-kB^2 l^2 / (4 m)) Lx Ly
+    const float c = 0.25f * kb2 * l * l;
+    for (int m0 = m_lo; m0 <= m_hi; m0 += 64) {
+      float P = poisson_anchor(m0, x);
+      const int m_end = min(m_hi, m0 + 63);
+      for (int m = m0; m <= m_end; ++m) {
+        const float mf = (float)m;
+        const float im = __fdividef(1.0f, mf);
+        if (m > m0) P *= x * im;
+        acc = __fmaf_rn(P * __expf(-c * im), im, acc);
+      }
+    }
+    acc *= 3.14159265359f * l * l * Lx * Ly;
   } else {
     const float l4 = (l * l) * (l * l);
-    for (int m = m_lo; m <= m_hi; ++m) {
-      const float mf = (float)m;
-      const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
-      const float w = __expf(e);
-      if (w == 0.0f) continue;
-      acc += w * (l4 / (mf * mf)) * f_factor32(fa, fL, mf, A0, Lx, l) *
-             f_factor32(fa, fL, mf, B0, Ly, l);
+    for (int m0 = m_lo; m0 <= m_hi; m0 += 64) {
+      float P = poisson_anchor(m0, x);
+      const int m_end = min(m_hi, m0 + 63);
+      for (int m = m0; m <= m_end; ++m) {
+        const float mf = (float)m;
+        if (m > m0) P *= x / mf;
+        if (P == 0.0f) continue;
+        acc += P * (l4 / (mf * mf)) * f_factor32(fa, fL, mf, A0, Lx, l) *
+               f_factor32(fa, fL, mf, B0, Ly, l);
+      }
     }
   }
   return fmaxf(acc, 0.0f);
@@ -258,43 +289,45 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
 
 // D_Phi and its derivative with respect to x = (sigma K)^2 (adjoint): each
 // series term P_m(x) W_m has d/dx = P_m W_m (m / x - 1), so
-// dD/dx = (sum_m m P_m W_m) / x - D.
+// dD/dx = (sum_m m P_m W_m) / x - D. Same anchored Poisson weights.
 template <int KIND>
 __device__ __forceinline__ float d_phi32_dx(int n_terms, const float *lg,
                                             const float *fa, float fL,
                                             float sigma, float l, float K,
                                             float A0, float B0, float Lx,
                                             float Ly, float &dDdx) {
+  (void)lg;
   dDdx = 0.0f;
   const float sk = sigma * K;
   const float x = sk * sk;
   if (!(x > 0.0f)) return 0.0f;
-  const float logx = __logf(x);
   const float kb2 = A0 * A0 + B0 * B0;
   int m_lo, m_hi;
   d_phi_range<KIND>(x, n_terms, m_lo, m_hi);
   float acc = 0.0f, accm = 0.0f;
-  for (int m = m_lo; m <= m_hi; ++m) {
-    const float mf = (float)m;
-    const float im = __fdividef(1.0f, mf);
-    const float e = __fmaf_rn(mf, logx, -lg[m]) - x;
-    float t;
-    if (KIND == SS_ROUGH_GAUSS_AREA) {
-      t = __expf(e - 0.25f * kb2 * l * l * im) *
-          (3.14159265359f * l * l * Lx * Ly * im);
-    } else if (KIND == SS_ROUGH_EXP_AREA) {
-      const float rs = rsqrtf(__fmaf_rn(kb2 * l * l, im * im, 1.0f));
-      t = __expf(e) * (6.28318530718f * l * l * Lx * Ly * im * im) * rs *
-          rs * rs;
-    } else {
-      const float w = __expf(e);
-      t = w == 0.0f ? 0.0f
-                    : w * ((l * l) * (l * l) * im * im) *
-                          f_factor32(fa, fL, mf, A0, Lx, l) *
-                          f_factor32(fa, fL, mf, B0, Ly, l);
+  for (int m0 = m_lo; m0 <= m_hi; m0 += 64) {
+    float P = poisson_anchor(m0, x);
+    const int m_end = min(m_hi, m0 + 63);
+    for (int m = m0; m <= m_end; ++m) {
+      const float mf = (float)m;
+      const float im = __fdividef(1.0f, mf);
+      if (m > m0) P *= x * im;
+      float t;
+      if (KIND == SS_ROUGH_GAUSS_AREA) {
+        t = P * __expf(-0.25f * kb2 * l * l * im) *
+            (3.14159265359f * l * l * Lx * Ly * im);
+      } else if (KIND == SS_ROUGH_EXP_AREA) {
+        const float rs = rsqrtf(__fmaf_rn(kb2 * l * l, im * im, 1.0f));
+        t = P * (6.28318530718f * l * l * Lx * Ly * im * im) * rs * rs * rs;
+      } else {
+        t = P == 0.0f ? 0.0f
+                      : P * ((l * l) * (l * l) * im * im) *
+                            f_factor32(fa, fL, mf, A0, Lx, l) *
+                            f_factor32(fa, fL, mf, B0, Ly, l);
+      }
+      acc += t;
+      accm = __fmaf_rn(mf, t, accm);
     }
-    acc += t;
-    accm = __fmaf_rn(mf, t, accm);
   }
   if (!(acc > 0.0f)) return 0.0f;
   dDdx = accm / x - acc;
