@@ -17,24 +17,24 @@
 //     centre), which keeps the facet's arrival direction -- and the sinc
 //     arguments k_j (r_hat . e) -- accurate to ~1e-8 rad;
 //   * facet lookups: the float32 mean-plane crossing gives the affine cell
-//     coordinate (formed as a double-float; the crossing itself carries
-//     ~2e-5 cells of float32 error); within 3e-4 cells of a rounding boundary the
-//     float64 mean-plane chain of the reference is re-run for that pair, so
-//     the lookups are the reference's integer decisions;
+//     coordinate (formed as a double-float; the crossing itself carries up
+//     to ~5e-5 cells of float32 error through three interfaces); within
+//     1.5e-4 cells of a rounding boundary the float64 mean-plane chain of
+//     the reference is re-run for that pair, so the lookups are the
+//     reference's integer decisions;
 //   * leg lengths, optical path, carrier phase (2 k0 opl mod 2 pi) and the
 //     fast-time bin in double-float. The optical path is stationary in the
 //     crossing positions along the interface (Fermat), so that float32
-//     error enters at second order; the crossing's float32 offset from the
-//     facet plane (up to ~1e-5 m for far crossings) enters at first order,
-//     and the sequential path adds it back (height from exact products
-//     times the legs' index-weighted cosines). A sequential chain through
-//     two or more interfaces is not stationary in its upper crossings, so
-//     their float32 in-plane error also enters at first order (~1e-5 m,
-//     rarely ~1e-4 m). A pair whose bin position
-//     lies within 5e-5 m of optical path (2e-4 m for such chains; at
-//     least 1e-6 bins) of a bin edge is re-evaluated with the complete
-//     float64 path, so bins equal the float64 form's also for the fine bins
-//     of the high bands;
+//     error enters at second order. The crossings' float32 offsets from the
+//     facet planes (up to ~1e-5 m for crossings far from the facet centre)
+//     enter at first order, and both paths add them back (height from
+//     exact products times the legs' index-weighted cosines): the optical
+//     path then agrees with the float64 form's to ~1e-9 m. A sequential
+//     chain through two or more interfaces is not stationary in its upper
+//     crossings, so their float32 in-plane error also enters at first order
+//     (~1e-5 m). A pair whose bin position lies within 1e-6 bins of a bin
+//     edge (for such chains, within 5e-5 m of optical path) is re-evaluated
+//     with the complete float64 path, so bins equal the float64 form's;
 //   * radiometry (Fresnel, spreading, attenuation, antenna gain, sinc,
 //     roughness series, diffuse channel) in float32.
 //
@@ -54,12 +54,14 @@ namespace ss {
 constexpr float kTiny32 = 1e-30f;
 constexpr float kEps32 = 1.1920929e-07f;
 constexpr float kTol32 = 1e-4f;
-constexpr float kLookupGuard = 3e-4f;
-// Bin-edge band: the larger of kBinGuard bins and kOplGuard metres of
-// optical path (several times the float32 crossing's first-order
-// optical-path error through up to four crossings).
+// Lookup guard band (cells): 3.3x the largest float32 cell-coordinate error
+// measured through three interfaces (4.5e-5 cells).
+constexpr float kLookupGuard = 1.5e-4f;
+// Bin-edge band: kBinGuard bins; for sequential chains through two or more
+// interfaces, the larger of that and kOplGuardChain metres of optical path
+// (~6x their largest float32 optical-path error, 8.6e-6 m).
 constexpr float kBinGuard = 1e-6f;
-constexpr double kOplGuard = 5e-5;
+constexpr double kOplGuardChain = 5e-5;
 
 // Per-interface constants of the float32 lookup pass.
 struct MeanPlane32 {
@@ -76,7 +78,7 @@ struct RefSplitConsts {
   float k0, amp_pref_j, kj, taper_inv, sigma, corr, fadL, n_exp;
   float K2h, K2l;             // 2 k0 as double-float
   float Ah, Al, Bh, Bl;       // u = opl A - B, A = 2/(c dt), B = t0/dt
-  float bin_guard;            // bin-edge band in bins (kBinGuard, kOplGuard)
+  float bin_guard;            // bin-edge band in bins (kBinGuard, kOplGuardChain)
   float n_leg[SS_MAX_IFACE + 1], n_leg_lo[SS_MAX_IFACE + 1],
       eps_leg[SS_MAX_IFACE + 1], att_leg[SS_MAX_IFACE + 1],
       sig_c[SS_MAX_IFACE];
@@ -403,7 +405,7 @@ __device__ __forceinline__ void path_sequential_split(const RefArgs &a,
 // ---------------------------------------------------------------------
 // joint solve (multilayer.py:408-457, refraction_joint.py:249-322)
 // ---------------------------------------------------------------------
-template <int NI, bool EXACT>
+template <int NI, bool EXACT, bool GRAD = false>
 __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
                                  const TraceS &T, const double *p64,
                                  const float *q, PathS &P) {
@@ -678,11 +680,27 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
     evan = evan || (nm[i] * st1 > nm[i + 1] * (1.0f + 64.0f * kEps32));
   }
   P.valid = (residual <= kTol32) && isfinite(residual) && sides && !evan;
+  // The crossings lie in the planes of the float32-normalised normals,
+  // up to ~1e-7 of their distance from the facet centre off the plane of
+  // the table's normal as stored, which the float64 form uses; the
+  // optical path takes that offset at first order (the in-plane error is
+  // second order: the joint path is stationary in every crossing). Moving
+  // crossing i onto the stored plane changes its two legs by hp c_in and
+  // -hp c_out, hp its height over that plane towards the upper point.
+  float dopl = 0.0f;
+  for (int i = 0; i < NI; ++i) {
+    const float *g =
+        a.ifc[i].table + ((size_t)rows[i] * a.ifc[i].nx + cols[i]) * 6;
+    const float tn[3] = {g[3], g[4], g[5]};
+    const float h = plane_height(Ym[i], tn);
+    const float hp = dot3a(Nn[i], dh[i]) <= 0.0f ? h : -h;
+    dopl += hp * (nm[i] * cinc[i] - nm[i + 1] * cout_[i]);
+  }
   // radiometry sums and optical path (multilayer.py:436-457)
   float c_inc[NI];
   for (int i = 0; i < NI; ++i) c_inc[i] = fmaxf(cinc[i], (float)kCMin);
   const float c_surf = c_inc[a.k_pad];
-  float tau2 = 1.0f, loss = 0.0f, sperp = 0.0f, spar = 0.0f;
+  float tau2 = 1.0f, loss = 0.0f, sperp = 0.0f, spar = 0.0f, dloss = 0.0f;
   df opl = df_make(0.0f, 0.0f);
   for (int i = 0; i < NI; ++i) {
     const float g = fresnel_gamma32(k.eps_leg[i], k.eps_leg[i + 1], c_inc[i]);
@@ -696,12 +714,14 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
     const float si = S[i].hi;
     opl = df_add(opl, df_mul(S[i], df_make(k.n_leg[i], k.n_leg_lo[i])));
     loss += si * (k.att_leg[i] * 1e-3f);
+    if (GRAD) dloss += si * (k.att_mask[i] * 1e-3f);
     sperp += si / nm[i];
     spar += si / (nm[i] * cp * cp);
   }
   P.tau2 = tau2;
-  P.opl = opl;
+  P.opl = df_add_f(opl, dopl);
   P.loss_db = loss;
+  P.dloss = dloss;
   P.sum_perp = sperp;
   P.sum_par = spar;
   P.c0 = c_surf;
@@ -759,7 +779,7 @@ __device__ __forceinline__ bool pair_eval(
   if (NI == 0)
     path_sequential_split<EXACT, GRAD>(a, k, T, p64, q, P);
   else
-    path_joint_split<NI == 0 ? 1 : NI, EXACT>(a, k, T, p64, q, P);
+    path_joint_split<NI == 0 ? 1 : NI, EXACT, GRAD>(a, k, T, p64, q, P);
   if (!EXACT && P.defer) return false;
   const int nj = a.leg_last;
   const float n0 = k.n_leg[0], njn = k.n_leg[nj];
