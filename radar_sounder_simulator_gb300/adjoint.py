@@ -2,8 +2,9 @@
 ``torch.autograd.Function``.
 
 The reference has no gradient code; this module adds one for the refracted
-target path of ``kernels/multilayer.py:594-770`` (sequential refraction,
-coherent mode). ``WindowPowerModel`` fixes the scene, track and instrument;
+target path of ``kernels/multilayer.py:594-770`` (coherent mode; the
+sequential chain or the joint solve of ``refraction_joint.py:249-322``).
+``WindowPowerModel`` fixes the scene, track and instrument;
 its differentiable map
 
     (reflectivity_db (N,), rms_height (N,), alpha) -> P (T,)
@@ -14,7 +15,8 @@ field, P_t = sum_{b in window} |F_t[b]|^2, with
 * reflectivity_db: per-facet reflection coefficient in dB, gamma = 10^(R/20);
 * rms_height: per-facet roughness rms height sigma (the rough-facet model
   of ``kernels/coherent.py:131-168``, series of ``roughness.py:127-186``);
-* alpha: attenuation rate (dB/km) of the legs listed in ``alpha_legs``.
+* alpha: attenuation rate (dB/km) of the legs listed in ``alpha_legs``
+  (indices into the caller's ``att_leg``).
 
 Forward: ``ss_refracted_fwd`` (split form, or the FP64 form). Backward:
 ``ss_refracted_adjoint`` recomputes every (trace, facet) phasor from the
@@ -39,8 +41,9 @@ class WindowPowerModel:
     def __init__(self, positions, u_ct, target, crossed, eps_leg, att_leg, *,
                  t0, dt, n_samples, c, k0, window, alpha_legs,
                  corr_length, phasors, n_terms, acf="exponential",
-                 d_phi_area=True, taper_s=0.05, precision="split",
-                 device=None):
+                 d_phi_area=True, taper_s=0.05, refraction="sequential",
+                 pad_to=None, joint_newton=6, joint_backtrack=4,
+                 precision="split", device=None):
         n = np.asarray(target.centers).shape[0]
         self.N = n
         self.window = (int(window[0]), int(window[1]))
@@ -50,13 +53,17 @@ class WindowPowerModel:
             mode="coherent", t0=t0, dt=dt, n_samples=n_samples, c=c,
             gamma=np.ones(n), k0=k0,
             roughness=(np.full(n, 0.1), corr_length, phasors, n_terms, acf),
-            d_phi_area=d_phi_area, taper_s=taper_s,
-            refraction="sequential", precision=precision, device=device)
+            d_phi_area=d_phi_area, taper_s=taper_s, refraction=refraction,
+            pad_to=pad_to, joint_newton=joint_newton,
+            joint_backtrack=joint_backtrack, precision=precision,
+            device=device)
         self.device = self.plan.device
         self.order = torch.as_tensor(self.plan.cull.order, device=self.device)
+        # the joint solve pads air planes (and legs) above the surface
+        self.k_pad = int(self.plan.opts.k_pad) if refraction == "joint" else 0
         mask = np.zeros(len(self.plan.legs[2]))
         for leg in self.alpha_legs:
-            mask[leg] = 1.0
+            mask[leg + self.k_pad] = 1.0
         self.alpha_mask = np.ascontiguousarray(mask, np.float64)
         self.scratch = None
         lo, hi = self.window
@@ -72,7 +79,7 @@ class WindowPowerModel:
         ex["sigma"].copy_(s[self.order])
         a = float(alpha)
         for leg in self.alpha_legs:
-            self.plan.legs[2][leg] = a
+            self.plan.legs[2][leg + self.k_pad] = a
 
     def forward_field(self, reflectivity_db, rms_height, alpha):
         """Target field (T, n_samples, 2) float64 for these parameters."""

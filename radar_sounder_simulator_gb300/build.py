@@ -68,7 +68,7 @@ def build(force=False, verbose=False):
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")
         return obj
 
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 2)) as ex:
+    with cf.ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 2)) as ex:
         objs = list(ex.map(compile_one, sources()))
     tmp = LIB + ".tmp"
     cmd = [cc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]

@@ -289,7 +289,9 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
 
 // D_Phi and its derivative with respect to x = (sigma K)^2 (adjoint): each
 // series term P_m(x) W_m has d/dx = P_m W_m (m / x - 1), so
-// dD/dx = (sum_m m P_m W_m) / x - D. Same anchored Poisson weights.
+// dD/dx = sum_m (m - x) P_m W_m / x, accumulated with the factor (m - x)
+// itself (the form sum m P W / x - D cancels to ~1/sqrt(x) of its terms
+// near the Poisson peak). Same anchored Poisson weights as d_phi32.
 template <int KIND>
 __device__ __forceinline__ float d_phi32_dx(int n_terms, const float *lg,
                                             const float *fa, float fL,
@@ -304,33 +306,52 @@ __device__ __forceinline__ float d_phi32_dx(int n_terms, const float *lg,
   const float kb2 = A0 * A0 + B0 * B0;
   int m_lo, m_hi;
   d_phi_range<KIND>(x, n_terms, m_lo, m_hi);
-  float acc = 0.0f, accm = 0.0f;
-  for (int m0 = m_lo; m0 <= m_hi; m0 += 64) {
-    float P = poisson_anchor(m0, x);
-    const int m_end = min(m_hi, m0 + 63);
-    for (int m = m0; m <= m_end; ++m) {
-      const float mf = (float)m;
-      const float im = __fdividef(1.0f, mf);
-      if (m > m0) P *= x * im;
-      float t;
-      if (KIND == SS_ROUGH_GAUSS_AREA) {
-        t = P * __expf(-0.25f * kb2 * l * l * im) *
-            (3.14159265359f * l * l * Lx * Ly * im);
-      } else if (KIND == SS_ROUGH_EXP_AREA) {
-        const float rs = rsqrtf(__fmaf_rn(kb2 * l * l, im * im, 1.0f));
-        t = P * (6.28318530718f * l * l * Lx * Ly * im * im) * rs * rs * rs;
-      } else {
-        t = P == 0.0f ? 0.0f
-                      : P * ((l * l) * (l * l) * im * im) *
-                            f_factor32(fa, fL, mf, A0, Lx, l) *
-                            f_factor32(fa, fL, mf, B0, Ly, l);
+  float acc = 0.0f, accd = 0.0f;
+  if (KIND == SS_ROUGH_EXP_AREA) {
+    const float kl2 = kb2 * l * l;
+    for (int m0 = m_lo; m0 <= m_hi; m0 += 64) {
+      float mf = (float)m0;
+      float P = poisson_anchor(m0, x);
+      const int m_end = min(m_hi, m0 + 63);
+      for (int m = m0; m <= m_end; ++m) {
+        const float im = __fdividef(1.0f, mf);
+        if (m > m0) P *= x * im;
+        const float im2 = im * im;
+        const float rs = rsqrtf(__fmaf_rn(kl2, im2, 1.0f));
+        const float t = P * im2 * (rs * rs * rs);
+        acc += t;
+        accd = __fmaf_rn(mf - x, t, accd);
+        mf += 1.0f;
       }
-      acc += t;
-      accm = __fmaf_rn(mf, t, accm);
+    }
+    const float pref = 6.28318530718f * l * l * Lx * Ly;
+    acc *= pref;
+    accd *= pref;
+  } else {
+    for (int m0 = m_lo; m0 <= m_hi; m0 += 64) {
+      float P = poisson_anchor(m0, x);
+      const int m_end = min(m_hi, m0 + 63);
+      for (int m = m0; m <= m_end; ++m) {
+        const float mf = (float)m;
+        const float im = __fdividef(1.0f, mf);
+        if (m > m0) P *= x * im;
+        float t;
+        if (KIND == SS_ROUGH_GAUSS_AREA) {
+          t = P * __expf(-0.25f * kb2 * l * l * im) *
+              (3.14159265359f * l * l * Lx * Ly * im);
+        } else {
+          t = P == 0.0f ? 0.0f
+                        : P * ((l * l) * (l * l) * im * im) *
+                              f_factor32(fa, fL, mf, A0, Lx, l) *
+                              f_factor32(fa, fL, mf, B0, Ly, l);
+        }
+        acc += t;
+        accd = __fmaf_rn(mf - x, t, accd);
+      }
     }
   }
   if (!(acc > 0.0f)) return 0.0f;
-  dDdx = accm / x - acc;
+  dDdx = accd / x;
   return acc;
 }
 
