@@ -453,6 +453,50 @@ int ss_coherent_batch_prepare(const ss_coherent_job *jobs, int32_t n_jobs,
 int ss_coherent_batch_run(const ss_batch_info *info, void *scratch,
                           void *stream);
 
+/* Batched refracted targets (no counterpart in the reference, whose
+ * simulate() calls refracted_cluttergram once per target layer and
+ * frequency band: simulate.py:338-381, the call at :373-379): one job per
+ * call of ss_refracted_fwd in split precision, all jobs of a batch on the
+ * same path class (the sequential chain, or the joint solve through the
+ * same number of interfaces after padding, at most 4), the same roughness
+ * kind and one antenna table. */
+typedef struct {
+  ss_refracted_opts opts;  /* host arrays (crossed, legs) read at prepare */
+  ss_facets target;
+  ss_traces traces;
+  ss_pattern pattern;      /* kind SS_PAT_ISOTROPIC for none */
+  ss_roughness rough;      /* kind SS_ROUGH_NONE for none */
+  ss_output out;
+} ss_refracted_job;
+
+/* Filled by ss_refracted_batch_prepare; passed back to
+ * ss_refracted_batch_run. */
+typedef struct {
+  int32_t n_jobs, path_class, rough_kind, plain, ctas, reserved;
+  int64_t n_items, n_out, n_words;
+  uint64_t smem, fix_smem, table_offset, mask_offset;
+} ss_refracted_batch_info;
+
+size_t ss_refracted_batch_scratch_bytes(const ss_refracted_job *jobs,
+                                        int32_t n_jobs,
+                                        const ss_batch_tuning *tune);
+
+/* Validates every job, lays out `scratch` (work-queue counter, job table,
+ * per-job partials and deferral masks) and uploads the job table
+ * (synchronous). The jobs' device pointers must stay valid while the batch
+ * is run. */
+int ss_refracted_batch_prepare(const ss_refracted_job *jobs, int32_t n_jobs,
+                               const ss_batch_tuning *tune, void *scratch,
+                               size_t scratch_bytes,
+                               ss_refracted_batch_info *info);
+
+/* Runs a prepared batch on `stream`: clears the masks, one persistent
+ * work-queue kernel over every job's (trace block x facet chunk) items, one
+ * batched fix-up of the deferred pairs, one batched reduce into every
+ * job's output. Stream operations only (graph-capturable). */
+int ss_refracted_batch_run(const ss_refracted_batch_info *info,
+                           void *scratch, void *stream);
+
 /* Pulse compression of kernel output along fast time. */
 typedef struct {
   int32_t n_traces;  /* T */

@@ -167,6 +167,22 @@ class TraceProductsOut(C.Structure):
         "nadir_index", "nadir_twtt", "first_index", "first_twtt")]
 
 
+class RefractedJob(C.Structure):
+    _fields_ = [("opts", RefractedOpts), ("target", Facets),
+                ("traces", Traces), ("pattern", Pattern),
+                ("rough", Roughness), ("out", Output)]
+
+
+class RefractedBatchInfo(C.Structure):
+    _fields_ = [("n_jobs", C.c_int32), ("path_class", C.c_int32),
+                ("rough_kind", C.c_int32), ("plain", C.c_int32),
+                ("ctas", C.c_int32), ("reserved", C.c_int32),
+                ("n_items", C.c_int64), ("n_out", C.c_int64),
+                ("n_words", C.c_int64), ("smem", C.c_uint64),
+                ("fix_smem", C.c_uint64), ("table_offset", C.c_uint64),
+                ("mask_offset", C.c_uint64)]
+
+
 class BatchInfo(C.Structure):
     _fields_ = [("n_jobs", C.c_int32), ("precision", C.c_int32),
                 ("rough_kind", C.c_int32), ("threads", C.c_int32),
@@ -223,6 +239,13 @@ SIGNATURES = {
     "ss_coherent_batch_prepare": (C.c_int, [
         C.POINTER(CoherentJob), C.c_int32, C.POINTER(BatchTuning),
         C.c_void_p, C.c_size_t, C.POINTER(BatchInfo)]),
+    "ss_refracted_batch_scratch_bytes": (C.c_size_t, [
+        C.POINTER(RefractedJob), C.c_int32, C.POINTER(BatchTuning)]),
+    "ss_refracted_batch_prepare": (C.c_int, [
+        C.POINTER(RefractedJob), C.c_int32, C.POINTER(BatchTuning),
+        C.c_void_p, C.c_size_t, C.POINTER(RefractedBatchInfo)]),
+    "ss_refracted_batch_run": (C.c_int, [C.POINTER(RefractedBatchInfo),
+                                         C.c_void_p, C.c_void_p]),
     "ss_coherent_batch_run": (C.c_int, [C.POINTER(BatchInfo), C.c_void_p,
                                         C.c_void_p]),
     "ss_incoherent_scratch_bytes": (C.c_size_t, [C.POINTER(IncoherentOpts),

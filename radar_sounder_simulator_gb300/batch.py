@@ -209,3 +209,112 @@ def coherent_batch(jobs, *, precision="split", tuning=None, autotune=False,
         b.autotune()
     b.run()
     return b.to_numpy(out_dtype)
+
+
+class RefractedBatch:
+    """Many ``prepare_refracted`` plans (split form) run as one persistent
+    launch: the reference's simulate() calls refracted_cluttergram once per
+    target layer and band (simulate.py:338-381); here every such call of
+    one path class (the sequential chain, or the joint solve through the
+    same interface count), roughness kind and antenna table shares one work
+    queue, one batched fix-up and one batched reduce."""
+
+    def __init__(self, plans, tuning=None):
+        if not plans:
+            raise ValueError("empty batch")
+        self.plans = list(plans)
+        self.device = self.plans[0].device
+        self.L = _lib.lib()
+        self.outputs = []
+        jobs = (_lib.RefractedJob * len(self.plans))()
+        for j, p in enumerate(self.plans):
+            p.opts.precision = _lib.PREC["split"]
+            field = torch.empty((p.T, p.n_seg, 2), dtype=torch.float64,
+                                device=self.device)
+            dropped = torch.empty(p.T, dtype=torch.float64,
+                                  device=self.device)
+            self.outputs.append((field, dropped))
+            jobs[j].opts = p.opts
+            jobs[j].target = p.fst
+            jobs[j].traces = p.tr
+            jobs[j].pattern = p.pst
+            jobs[j].rough = p.rst
+            jobs[j].out = _lib.Output(field.data_ptr(), None,
+                                      dropped.data_ptr())
+        self.jobs = jobs
+        self.scratch = None
+        self.prepare(tuning or (512, 8, 8, 0))
+
+    def prepare(self, tuning):
+        """Lay out scratch and upload the job table for ``tuning`` =
+        (threads: 512, max traces per item, items per SM, CTAs per SM)."""
+        t = BatchTuning(*[int(v) for v in tuning])
+        n = self.L.ss_refracted_batch_scratch_bytes(self.jobs, len(self.jobs),
+                                                    C.byref(t))
+        if n == 0:
+            msg = self.L.ss_last_error().decode(errors="replace")
+            raise ValueError(f"batch layout failed: {msg}")
+        if self.scratch is None or self.scratch.numel() < n:
+            self.scratch = torch.empty(n, dtype=torch.uint8,
+                                       device=self.device)
+        info = _lib.RefractedBatchInfo()
+        torch.cuda.synchronize(self.device)
+        st = self.L.ss_refracted_batch_prepare(
+            self.jobs, len(self.jobs), C.byref(t),
+            C.c_void_p(self.scratch.data_ptr()), n, C.byref(info))
+        _lib.check(st, "ss_refracted_batch_prepare")
+        self.info = info
+        self.tuning = tuple(int(v) for v in tuning)
+        return info
+
+    def kernel_launches(self):
+        """Library kernels one ``run()`` launches (persistent pass, batched
+        fix-up, batched reduce)."""
+        return 3
+
+    def run(self):
+        """Launch on the current stream; returns [(field, dropped)] per job
+        (device tensors, the ``RefractedPlan.run`` layout)."""
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        st = self.L.ss_refracted_batch_run(
+            C.byref(self.info), C.c_void_p(self.scratch.data_ptr()),
+            C.c_void_p(stream))
+        _lib.check(st, "ss_refracted_batch_run")
+        return self.outputs
+
+    def to_numpy(self, out_dtype=None):
+        return [p.to_numpy(f, d, out_dtype)
+                for p, (f, d) in zip(self.plans, self.outputs)]
+
+
+class BatchGraph:
+    """Several batches (and any other stream work) captured into one CUDA
+    graph, so a multi-layer, multi-band step is one replay: ``steps`` are
+    callables that only enqueue device work on the current stream (e.g.
+    ``CoherentBatch.run``, ``RefractedBatch.run``, pulse compression)."""
+
+    def __init__(self, steps, device=None):
+        self.steps = list(steps)
+        self.device = torch.device(device or "cuda")
+        self.graph = None
+
+    def run(self):
+        for fn in self.steps:
+            fn()
+
+    def capture(self):
+        s = torch.cuda.Stream(self.device)
+        s.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(s):
+            self.run()          # eager warm-up on a side stream
+        torch.cuda.current_stream(self.device).wait_stream(s)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g):
+            self.run()
+        self.graph = g
+        return g
+
+    def replay(self):
+        if self.graph is None:
+            self.capture()
+        self.graph.replay()

@@ -67,6 +67,13 @@ RefSplitConsts split_consts(const RefArgs &a) {
   return k;
 }
 
+// Dynamic shared memory of the fast kernel: the trace block's histograms
+// and the series table.
+size_t split_smem_bytes(const RefArgs &a, int tb) {
+  return (size_t)tb * a.n_seg * sizeof(float2) +
+         (a.rough_kind ? (a.n_terms + 1) * sizeof(float) : 0);
+}
+
 int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
   int pa_len, pb_len;
   pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
@@ -80,8 +87,7 @@ int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
     return SS_ERR_UNSUPPORTED;
   }
   const RefSplitConsts k = split_consts(a);
-  const size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2) +
-                      (a.rough_kind ? (a.n_terms + 1) * sizeof(float) : 0);
+  const size_t smem = split_smem_bytes(a, p.tb);
   if (!a.joint) return split_launch_ni0(a, k, p, smem, st);
   switch (a.ni) {
     case 1: return split_launch_ni1(a, k, p, smem, st);

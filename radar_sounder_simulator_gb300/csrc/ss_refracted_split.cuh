@@ -921,17 +921,16 @@ __device__ __forceinline__ bool pair_eval(
   return true;
 }
 
-// Fast kernel: CTA = (facet chunk, trace block); thread <-> facet; per-trace
-// histograms in shared memory; pairs that need a float64 decision are marked
-// in the deferral bitmask (bit t * defer_w + (i - lo_t)).
-// Up to two crossings the solve fits 64 registers, so two 512-thread CTAs
-// share an SM (32 warps; the joint solve through two interfaces spills a
-// few words at that budget and still gains 8%); through three or more it
-// keeps ~125 registers and one CTA.
+// One CTA's work item of the fast kernel: facet chunk `chunk` of trace
+// block `group`; thread <-> facet; per-trace histograms in shared memory;
+// pairs that need a float64 decision are marked in the deferral bitmask
+// (bit t * defer_w + (i - lo_t)). Shared by the one-call kernel (item =
+// block index) and the batched persistent kernel (item from a work queue).
 template <int NI, int ROUGH, bool PLAIN>
-__global__ void __launch_bounds__(kSplitThreads, NI >= 3 ? 1 : 2)
-refracted_split_kernel(RefArgs a, RefSplitConsts k) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void refracted_split_cta(const RefArgs &a,
+                                                    const RefSplitConsts &k,
+                                                    int chunk, int group,
+                                                    unsigned char *smem_raw) {
   float2 *hist = reinterpret_cast<float2 *>(smem_raw);
   float *lg = reinterpret_cast<float *>(hist + (size_t)a.tb * a.n_seg);
   __shared__ double s_p64[SS_MAX_TB][3];
@@ -943,8 +942,7 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   __shared__ float s_fad[SS_FAD_N];
   __shared__ int s_rng[2];
   __shared__ int s_next;
-  const int chunk = blockIdx.x;
-  const int t_base = blockIdx.y * a.tb;
+  const int t_base = group * a.tb;
   const int nt = min(a.tb, a.T - t_base);
   const int tid = threadIdx.x;
   int pa_len, pb_len;
@@ -999,9 +997,8 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
       if (i < s_lo[tt] || i >= s_hi[tt]) continue;
       PairOut o;
       if (!pair_eval<NI, ROUGH, false, false, PLAIN>(
-              a, k, s_tr[tt], s_p64[tt], s_u[tt],
-                                       s_pv[tt], s_pat, pa_len, lg, s_fad, i,
-                                       q, o)) {
+              a, k, s_tr[tt], s_p64[tt], s_u[tt], s_pv[tt], s_pat, pa_len,
+              lg, s_fad, i, q, o)) {
         const unsigned long long bit =
             (unsigned long long)(t_base + tt) * a.defer_w + (i - s_lo[tt]);
         atomicOr(&a.defer_mask[bit >> 5], 1u << (bit & 31));
@@ -1025,6 +1022,19 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
   }
   if (tid < nt)
     a.part_drop[(size_t)chunk * a.T + t_base + tid] = (double)s_drop[tid];
+}
+
+// Fast kernel: one CTA per (facet chunk, trace block).
+// Up to two crossings the solve fits 64 registers, so two 512-thread CTAs
+// share an SM (32 warps; the joint solve through two interfaces spills a
+// few words at that budget and still gains 8%); through three or more it
+// keeps ~125 registers and one CTA.
+template <int NI, int ROUGH, bool PLAIN>
+__global__ void __launch_bounds__(kSplitThreads, NI >= 3 ? 1 : 2)
+refracted_split_kernel(RefArgs a, RefSplitConsts k) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  refracted_split_cta<NI, ROUGH, PLAIN>(a, k, blockIdx.x, blockIdx.y,
+                                        smem_raw);
 }
 
 // Fix-up kernel: evaluates the deferred pairs with the float64 decisions
@@ -1174,8 +1184,223 @@ inline int launch_split_r(RefArgs &a, const RefSplitConsts &k, const Plan &p,
   }
 }
 
+// ---------------------------------------------------------------------
+// batched refracted targets: one persistent work-queue launch for many
+// jobs of one path class (crossed-interface count), roughness kind and
+// form, then one batched fix-up and one batched reduce
+// ---------------------------------------------------------------------
+struct RefBatchJob {
+  RefArgs a;
+  RefSplitConsts k;
+  long long item0;  // first work item (trace block x facet chunk)
+  long long out0;   // first reduce element (trace x segment)
+  long long word0;  // first deferral-mask word (multiple of 32)
+  long long words;  // this job's mask words
+  int n_chunks, n_groups;
+  ss_output out;
+};
+
+// Index of the job owning position `x` of a prefix field (first <= x).
+template <int FIELD>
+__device__ __forceinline__ int ref_batch_find(const RefBatchJob *jobs,
+                                              int n_jobs, long long x) {
+  int lo = 0, hi = n_jobs - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    const long long f = FIELD == 0 ? jobs[mid].item0
+                                   : FIELD == 1 ? jobs[mid].out0
+                                                : jobs[mid].word0;
+    if (f <= x) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int NI, int ROUGH, bool PLAIN>
+__global__ void __launch_bounds__(kSplitThreads, NI >= 3 ? 1 : 2)
+refracted_batch_kernel(const RefBatchJob *jobs, int n_jobs,
+                       long long n_items, unsigned long long *counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ long long s_item;
+  __shared__ int s_job;
+  for (;;) {
+    __syncthreads();  // the previous item's shared memory is free
+    if (threadIdx.x == 0) {
+      const long long it = (long long)atomicAdd(counter, 1ull);
+      s_item = it;
+      s_job = it < n_items ? ref_batch_find<0>(jobs, n_jobs, it) : 0;
+    }
+    __syncthreads();
+    const long long it = s_item;
+    if (it >= n_items) break;
+    const RefBatchJob &J = jobs[s_job];
+    const long long local = it - J.item0;
+    refracted_split_cta<NI, ROUGH, PLAIN>(J.a, J.k,
+                                          (int)(local % J.n_chunks),
+                                          (int)(local / J.n_chunks),
+                                          smem_raw);
+  }
+}
+
+// Batched fix-up: the jobs' masks are laid end to end in 32-word groups,
+// so each warp's 32-word scan belongs to one job; queued bits carry their
+// job. The jobs share one antenna table (staged once).
+template <int NI, int ROUGH>
+__global__ void __launch_bounds__(32 * kFixWarps)
+refracted_batch_fixup(const RefBatchJob *jobs, int n_jobs,
+                      long long n_words) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float *lg = reinterpret_cast<float *>(smem_raw);
+  __shared__ float s_pat[SS_PAT_MAX];
+  __shared__ float s_fad[SS_FAD_N];
+  __shared__ unsigned long long s_q[kFixWarps][kFixQueue];
+  __shared__ int s_qj[kFixWarps][kFixQueue];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const RefArgs &a0 = jobs[0].a;
+  int pa_len, pb_len;
+  pattern_lengths(a0.pat_kind, a0.pat_n, pa_len, pb_len);
+  for (int j = tid; j < pa_len; j += blockDim.x) s_pat[j] = (float)a0.pa[j];
+  for (int j = tid; j < pb_len; j += blockDim.x)
+    s_pat[pa_len + j] = (float)a0.pb[j];
+  if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
+    s_fad[tid] = (float)a0.fad.a[tid];
+  __syncthreads();
+  const unsigned long long n_warps =
+      (unsigned long long)gridDim.x * kFixWarps;
+  unsigned long long *q = s_q[warp];
+  int *qj = s_qj[warp];
+  int qn = 0;
+  auto eval = [&](unsigned long long bit, int jb) {
+    const RefBatchJob &J = jobs[jb];
+    fixup_pair<NI, ROUGH>(J.a, J.k, bit, s_pat, pa_len, lg, s_fad);
+  };
+  for (unsigned long long base =
+           ((unsigned long long)blockIdx.x * kFixWarps + warp) * 32;
+       base < (unsigned long long)n_words; base += n_warps * 32) {
+    const int jb = ref_batch_find<2>(jobs, n_jobs, (long long)base);
+    const RefBatchJob &J = jobs[jb];
+    const long long lw = (long long)base - J.word0 + lane;
+    unsigned int m = lw < J.words ? J.a.defer_mask[lw] : 0u;
+    const int c = __popc(m);
+    int incl = c;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int pos = qn + incl - c;
+    while (m) {
+      const int b = __ffs(m) - 1;
+      m &= m - 1;
+      qj[pos] = jb;
+      q[pos++] = ((unsigned long long)lw << 5) + b;
+    }
+    __syncwarp();
+    qn += total;
+    while (qn >= 32) {
+      const unsigned long long bit = q[qn - 32 + lane];
+      const int jq = qj[qn - 32 + lane];
+      __syncwarp();
+      eval(bit, jq);
+      qn -= 32;
+    }
+    __syncwarp();
+  }
+  if (lane < qn) eval(q[lane], qj[lane]);
+}
+
+// Persistent pass and fix-up of one path class (NI = 0: sequential).
+#define SS_REF_BATCH_DECL(N)                                                \
+  int refracted_batch_launch_ni##N(                                         \
+      const RefBatchJob *jobs, int n_jobs, long long n_items,              \
+      long long n_words, unsigned long long *counter, int rough_kind,      \
+      bool plain, int ctas, size_t smem, size_t fix_smem, cudaStream_t st); \
+  int refracted_batch_occupancy_ni##N(int rough_kind, bool plain,          \
+                                      size_t smem);
+SS_REF_BATCH_DECL(0)
+SS_REF_BATCH_DECL(1)
+SS_REF_BATCH_DECL(2)
+SS_REF_BATCH_DECL(3)
+SS_REF_BATCH_DECL(4)
+#undef SS_REF_BATCH_DECL
+
+// Launch helpers instantiated in each path class's translation unit.
+template <int NI, int ROUGH, bool PLAIN>
+inline int ref_batch_launch_t(const RefBatchJob *jobs, int n_jobs,
+                              long long n_items, long long n_words,
+                              unsigned long long *counter, int ctas,
+                              size_t smem, size_t fix_smem,
+                              cudaStream_t st) {
+  refracted_batch_kernel<NI, ROUGH, PLAIN><<<ctas, kSplitThreads, smem, st>>>(
+      jobs, n_jobs, n_items, counter);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "refracted batch launch");
+  const unsigned long long want =
+      ((unsigned long long)n_words + 32 * kFixWarps - 1) / (32 * kFixWarps);
+  const int blocks = (int)std::max<unsigned long long>(
+      1, std::min<unsigned long long>(want, 8ull * sm_count()));
+  refracted_batch_fixup<NI, ROUGH><<<blocks, 32 * kFixWarps, fix_smem, st>>>(
+      jobs, n_jobs, n_words);
+  return cuda_status(cudaGetLastError(), "refracted batch fix-up launch");
+}
+
+template <int NI>
+inline int ref_batch_launch_r(const RefBatchJob *jobs, int n_jobs,
+                              long long n_items, long long n_words,
+                              unsigned long long *counter, int rough_kind,
+                              bool plain, int ctas, size_t smem,
+                              size_t fix_smem, cudaStream_t st) {
+  switch (rough_kind) {
+    case SS_ROUGH_NONE:
+      return plain ? ref_batch_launch_t<NI, SS_ROUGH_NONE, true>(
+                         jobs, n_jobs, n_items, n_words, counter, ctas, smem,
+                         fix_smem, st)
+                   : ref_batch_launch_t<NI, SS_ROUGH_NONE, false>(
+                         jobs, n_jobs, n_items, n_words, counter, ctas, smem,
+                         fix_smem, st);
+    case SS_ROUGH_GAUSS_FULL:
+      return ref_batch_launch_t<NI, SS_ROUGH_GAUSS_FULL, false>(
+          jobs, n_jobs, n_items, n_words, counter, ctas, smem, fix_smem, st);
+    case SS_ROUGH_GAUSS_AREA:
+      return ref_batch_launch_t<NI, SS_ROUGH_GAUSS_AREA, false>(
+          jobs, n_jobs, n_items, n_words, counter, ctas, smem, fix_smem, st);
+    default:
+      return ref_batch_launch_t<NI, SS_ROUGH_EXP_AREA, false>(
+          jobs, n_jobs, n_items, n_words, counter, ctas, smem, fix_smem, st);
+  }
+}
+
+template <int NI>
+inline int ref_batch_occupancy(int rough_kind, bool plain, size_t smem) {
+  int n = 0;
+  cudaError_t e = cudaSuccess;
+  auto one = [&](auto kern) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern,
+                                                        kSplitThreads, smem);
+  };
+  switch (rough_kind) {
+    case SS_ROUGH_NONE:
+      if (plain) one(refracted_batch_kernel<NI, SS_ROUGH_NONE, true>);
+      else one(refracted_batch_kernel<NI, SS_ROUGH_NONE, false>);
+      break;
+    case SS_ROUGH_GAUSS_FULL:
+      one(refracted_batch_kernel<NI, SS_ROUGH_GAUSS_FULL, false>);
+      break;
+    case SS_ROUGH_GAUSS_AREA:
+      one(refracted_batch_kernel<NI, SS_ROUGH_GAUSS_AREA, false>);
+      break;
+    default:
+      one(refracted_batch_kernel<NI, SS_ROUGH_EXP_AREA, false>);
+  }
+  return e == cudaSuccess ? n : 0;
+}
+
 // float32 / double-float constants of the split kernels.
 RefSplitConsts split_consts(const RefArgs &a);
+// Dynamic shared memory of the fast kernel for a trace block of tb.
+size_t split_smem_bytes(const RefArgs &a, int tb);
 
 // Fast + fix-up launches of one crossed-interface count (NI = 0: the
 // sequential path), each instantiated in its own translation unit.
