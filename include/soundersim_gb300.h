@@ -190,7 +190,11 @@ int ss_coherent_fwd_noalloc(const ss_coherent_opts *opts,
 
 /* ---- refracted multilayer facet sum ---------------------------------- */
 
-#define SS_MAX_IFACE 8  /* crossed interfaces per call (after padding) */
+/* Crossed interfaces per call after padding: the reference's deepest firn
+ * runs cross 40 layers. Above 4 (split form) or 8 (FP64 form) interfaces the
+ * joint solve keeps its per-interface arrays in local memory, which the
+ * driver reserves for every resident thread while such a call runs. */
+#define SS_MAX_IFACE 40
 
 /* One crossed interface: its facet lookup table and mean plane
  * (multilayer.py:269-283 `_grid_consts`; joint no-op pads per :286-330 are

@@ -281,7 +281,7 @@ int build_ref_args(const ss_refracted_opts *opts,
   int s = refracted_plan(opts, T, N, &p);
   if (s) {
     set_error(s == SS_ERR_UNSUPPORTED ? "n_samples too large" :
-              "bad sizes or crossed-interface count (1..8)");
+              "bad sizes or crossed-interface count (1..40)");
     return s;
   }
   if (opts->joint && (opts->k_pad < 0 || opts->k_pad >= opts->n_crossed)) {
@@ -418,7 +418,10 @@ extern "C" int ss_refracted_fwd(const ss_refracted_opts *opts,
       case 5: s = launch_fp64<5>(a, p, smem, st); break;
       case 6: s = launch_fp64<6>(a, p, smem, st); break;
       case 7: s = launch_fp64<7>(a, p, smem, st); break;
-      default: s = launch_fp64<8>(a, p, smem, st); break;
+      case 8: s = launch_fp64<8>(a, p, smem, st); break;
+      // deeper stacks (firn runs cross tens of layers): one instantiation
+      // whose joint-solve arrays hold SS_MAX_IFACE interfaces
+      default: s = launch_fp64<kDeepNI>(a, p, smem, st); break;
     }
   } else {
     s = refracted_split_launch(a, p, st);

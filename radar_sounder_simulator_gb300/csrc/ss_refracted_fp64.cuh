@@ -9,6 +9,10 @@ namespace ss {
 constexpr double kTiny = 1e-30;
 constexpr double kEps64 = 2.220446049250313e-16;
 constexpr double kCMin = 1e-9;
+// Template argument of the deep-stack instantiations: the joint solve's
+// arrays hold SS_MAX_IFACE interfaces (in local memory) and the count
+// crossed is the call's; every smaller argument is a count of its own.
+constexpr int kDeepNI = SS_MAX_IFACE;
 
 struct Snell64 {
   double x[3];
@@ -132,14 +136,14 @@ __device__ __forceinline__ void joint_geom(const double (&B)[NI][3][2],
                                            const double *ps, const double *qs,
                                            const double *nm,
                                            const double (&ab)[NI][2],
-                                           JointGeom<NI> &G) {
-  for (int i = 0; i < NI; ++i)
+                                           JointGeom<NI> &G, int ni = NI) {
+  for (int i = 0; i < ni; ++i)
     for (int k = 0; k < 3; ++k)
       G.x[i][k] = os[i][k] + (B[i][k][0] * ab[i][0] + B[i][k][1] * ab[i][1]);
   double g[NI + 1][3];
-  for (int k = 0; k <= NI; ++k) {
+  for (int k = 0; k <= ni; ++k) {
     const double *a = k == 0 ? ps : G.x[k - 1];
-    const double *b = k == NI ? qs : G.x[k];
+    const double *b = k == ni ? qs : G.x[k];
     double d[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
     G.s[k] = fmax(sqrt(dot3v(d, d)), kTiny);
     for (int j = 0; j < 3; ++j) {
@@ -147,7 +151,7 @@ __device__ __forceinline__ void joint_geom(const double (&B)[NI][3][2],
       g[k][j] = nm[k] * G.dh[k][j];
     }
   }
-  for (int i = 0; i < NI; ++i)
+  for (int i = 0; i < ni; ++i)
     for (int j = 0; j < 2; ++j) {
       double acc = 0.0;
       for (int k = 0; k < 3; ++k) acc += B[i][k][j] * (g[i][k] - g[i + 1][k]);
@@ -170,12 +174,13 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
                         const double (&O)[NI][3], const double (&Nn)[NI][3],
                         const double *nm, int n_newton, int n_backtrack,
                         double (&X)[NI][3], double (&th1)[NI],
-                        double (&th2)[NI], double (&S)[NI + 1], bool &valid) {
+                        double (&th2)[NI], double (&S)[NI + 1], bool &valid,
+                        int ni = NI) {
   // chain initialiser: refraction.py two-point form, 25 iterations
   double x0[NI][3];
   {
     double cur[3] = {p[0], p[1], p[2]};
-    for (int i = 0; i < NI; ++i) {
+    for (int i = 0; i < ni; ++i) {
       Snell64 R;
       snell64(cur, q, O[i], Nn[i], nm[i], nm[i + 1], 25, false, R);
       for (int j = 0; j < 3; ++j) x0[i][j] = cur[j] = R.x[j];
@@ -189,11 +194,11 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
     ps[j] = p[j] * inv;
     qs[j] = q[j] * inv;
   }
-  for (int i = 0; i < NI; ++i)
+  for (int i = 0; i < ni; ++i)
     for (int j = 0; j < 3; ++j) os[i][j] = O[i][j] * inv;
   // in-plane bases (refraction_joint.py:196-204)
   double B[NI][3][2];
-  for (int i = 0; i < NI; ++i) {
+  for (int i = 0; i < ni; ++i) {
     const double *n = Nn[i];
     const bool use_z = fabs(n[2]) < 0.9;
     const double a0 = use_z ? 0.0 : 1.0, a2 = use_z ? 1.0 : 0.0;
@@ -209,7 +214,7 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
     }
   }
   double ab[NI][2];
-  for (int i = 0; i < NI; ++i)
+  for (int i = 0; i < ni; ++i)
     for (int j = 0; j < 2; ++j) {
       double acc = 0.0;
       for (int k = 0; k < 3; ++k)
@@ -219,16 +224,16 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
   const double mu = pow(kEps64, 0.75);
   JointGeom<NI> G;
   for (int it = 0; it < n_newton; ++it) {
-    joint_geom<NI>(B, os, ps, qs, nm, ab, G);
-    // W_k = (n_k / s_k) (I - d d^T), k = 0..NI
+    joint_geom<NI>(B, os, ps, qs, nm, ab, G, ni);
+    // W_k = (n_k / s_k) (I - d d^T), k = 0..ni
     double W[NI + 1][3][3];
-    for (int k = 0; k <= NI; ++k)
+    for (int k = 0; k <= ni; ++k)
       for (int r = 0; r < 3; ++r)
         for (int c = 0; c < 3; ++c)
           W[k][r][c] = (nm[k] / G.s[k]) *
                        ((r == c ? 1.0 : 0.0) - G.dh[k][r] * G.dh[k][c]);
     double A[NI][2][2], Cm[NI > 1 ? NI - 1 : 1][2][2];
-    for (int i = 0; i < NI; ++i)
+    for (int i = 0; i < ni; ++i)
       for (int r = 0; r < 2; ++r)
         for (int c = 0; c < 2; ++c) {
           double acc = 0.0;
@@ -237,7 +242,7 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
               acc += B[i][k][r] * (W[i][k][l] + W[i + 1][k][l]) * B[i][l][c];
           A[i][r][c] = acc + (r == c ? mu : 0.0);
         }
-    for (int i = 0; i + 1 < NI; ++i)
+    for (int i = 0; i + 1 < ni; ++i)
       for (int r = 0; r < 2; ++r)
         for (int c = 0; c < 2; ++c) {
           double acc = 0.0;
@@ -248,7 +253,7 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
         }
     // block Thomas (refraction_joint.py:218-246)
     double dinv[NI][2][2], y[NI][2], delta[NI][2];
-    for (int i = 0; i < NI; ++i) {
+    for (int i = 0; i < ni; ++i) {
       double M[2][2], rhs[2] = {-G.f[i][0], -G.f[i][1]};
       if (i == 0) {
         for (int r = 0; r < 2; ++r)
@@ -270,43 +275,43 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
       y[i][0] = rhs[0];
       y[i][1] = rhs[1];
     }
-    for (int i = NI - 1; i >= 0; --i) {
+    for (int i = ni - 1; i >= 0; --i) {
       double rr[2] = {y[i][0], y[i][1]};
-      if (i < NI - 1)
+      if (i < ni - 1)
         for (int r = 0; r < 2; ++r)
           rr[r] -= Cm[i][r][0] * delta[i + 1][0] + Cm[i][r][1] * delta[i + 1][1];
       for (int r = 0; r < 2; ++r)
         delta[i][r] = dinv[i][r][0] * rr[0] + dinv[i][r][1] * rr[1];
     }
     double m0 = 0.0;
-    for (int i = 0; i < NI; ++i) m0 += G.f[i][0] * G.f[i][0] + G.f[i][1] * G.f[i][1];
+    for (int i = 0; i < ni; ++i) m0 += G.f[i][0] * G.f[i][0] + G.f[i][1] * G.f[i][1];
     double lam_sel = 0.0, lam = 1.0;
     for (int j = 0; j < n_backtrack; ++j, lam *= 0.5) {
       double cand[NI][2];
-      for (int i = 0; i < NI; ++i)
+      for (int i = 0; i < ni; ++i)
         for (int r = 0; r < 2; ++r) cand[i][r] = ab[i][r] + lam * delta[i][r];
       JointGeom<NI> Gc;
-      joint_geom<NI>(B, os, ps, qs, nm, cand, Gc);
+      joint_geom<NI>(B, os, ps, qs, nm, cand, Gc, ni);
       double mc = 0.0;
-      for (int i = 0; i < NI; ++i)
+      for (int i = 0; i < ni; ++i)
         mc += Gc.f[i][0] * Gc.f[i][0] + Gc.f[i][1] * Gc.f[i][1];
       if (mc < m0) {
         lam_sel = lam;
         break;
       }
     }
-    for (int i = 0; i < NI; ++i)
+    for (int i = 0; i < ni; ++i)
       for (int r = 0; r < 2; ++r) ab[i][r] += lam_sel * delta[i][r];
   }
-  joint_geom<NI>(B, os, ps, qs, nm, ab, G);
-  for (int i = 0; i < NI; ++i)
+  joint_geom<NI>(B, os, ps, qs, nm, ab, G, ni);
+  for (int i = 0; i < ni; ++i)
     for (int j = 0; j < 3; ++j) X[i][j] = G.x[i][j] * scale;
   // polyline geometry and validity (refraction_joint.py:143-176)
   double dh[NI + 1][3];
   bool fin = true;
-  for (int k = 0; k <= NI; ++k) {
+  for (int k = 0; k <= ni; ++k) {
     const double *a = k == 0 ? p : X[k - 1];
-    const double *b = k == NI ? q : X[k];
+    const double *b = k == ni ? q : X[k];
     double d[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
     S[k] = sqrt(dot3v(d, d));
     fin = fin && isfinite(S[k]);
@@ -315,7 +320,7 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
   }
   double residual = 0.0;
   bool sides = true, evan = false;
-  for (int i = 0; i < NI; ++i) {
+  for (int i = 0; i < ni; ++i) {
     const double *n = Nn[i];
     const double ct1 = dot3v(n, dh[i]), ct2 = dot3v(n, dh[i + 1]);
     double t1[3], t2[3], dG[3];
@@ -332,7 +337,7 @@ static __device__ __noinline__ void joint64(const double *p, const double *q,
     const double res = sqrt(dot3v(rt, rt));
     if (res > residual || isnan(res)) residual = res;
     const double *pa = i == 0 ? p : X[i - 1];
-    const double *pb = i == NI - 1 ? q : X[i + 1];
+    const double *pb = i == ni - 1 ? q : X[i + 1];
     double hpv[3] = {pa[0] - X[i][0], pa[1] - X[i][1], pa[2] - X[i][2]};
     double hnv[3] = {pb[0] - X[i][0], pb[1] - X[i][1], pb[2] - X[i][2]};
     sides = sides && (dot3v(n, hpv) * dot3v(n, hnv) < 0.0);
@@ -394,11 +399,14 @@ static __device__ __noinline__ void path_sequential64(const RefArgs &a, const do
 template <int NI>
 static __device__ __noinline__ void path_joint64(const RefArgs &a, const double *p,
                              const double *q, Path64 &P) {
+  // a deep stack (NI == kDeepNI) holds up to NI interfaces in its arrays
+  // and crosses a.ni of them; the other instantiations fold ni to NI
+  const int ni = NI == kDeepNI ? a.ni : NI;
   // pass 1: mean-plane chain (10 iterations) anchors the lookups
   double pt[NI][3], nr[NI][3];
   {
     double cur[3] = {p[0], p[1], p[2]};
-    for (int i = 0; i < NI; ++i) {
+    for (int i = 0; i < ni; ++i) {
       Snell64 R;
       snell64(cur, q, a.ifc[i].mean_point, a.ifc[i].mean_normal, a.n_leg[i],
               a.n_leg[i + 1], 10, false, R);
@@ -411,24 +419,24 @@ static __device__ __noinline__ void path_joint64(const RefArgs &a, const double 
   double X[NI][3], th1[NI], th2[NI], S[NI + 1];
   bool valid;
   joint64<NI>(p, q, pt, nr, a.n_leg, a.n_newton, a.n_backtrack, X, th1, th2,
-              S, valid);
+              S, valid, ni);
   P.valid = valid;
   double c_inc[NI];
-  for (int i = 0; i < NI; ++i) c_inc[i] = fmax(cos(th1[i]), kCMin);
+  for (int i = 0; i < ni; ++i) c_inc[i] = fmax(cos(th1[i]), kCMin);
   const double c_surf = c_inc[a.k_pad];
   double tau2 = 1.0, opl = 0.0, loss = 0.0, sperp = 0.0, spar = 0.0;
-  for (int i = 0; i < NI; ++i) {
+  for (int i = 0; i < ni; ++i) {
     const double g = fresnel_gamma64(a.eps_leg[i], a.eps_leg[i + 1], c_inc[i]);
     tau2 *= (1.0 - g * g);
   }
   if (a.rough_cross)
-    for (int i = 0; i < NI; ++i) {
+    for (int i = 0; i < ni; ++i) {
       const double kt =
           a.k0 * (a.n_leg[i] * cos(th1[i]) - a.n_leg[i + 1] * cos(th2[i]));
       const double sk = a.sig_c[i] * kt;
       tau2 *= exp(-2.0 * (sk * sk));
     }
-  for (int i = 0; i < NI; ++i) {
+  for (int i = 0; i < ni; ++i) {
     const double cp = i < a.k_pad ? c_surf : c_inc[i];
     const double nl = a.n_leg[i];
     opl += nl * S[i];
@@ -442,9 +450,9 @@ static __device__ __noinline__ void path_joint64(const RefArgs &a, const double 
   P.sum_perp = sperp;
   P.sum_par = spar;
   P.c0 = c_surf;
-  P.c_last = fmax(cos(th2[NI - 1]), kCMin);
+  P.c_last = fmax(cos(th2[ni - 1]), kCMin);
   for (int j = 0; j < 3; ++j) {
-    P.cur[j] = X[NI - 1][j];
+    P.cur[j] = X[ni - 1][j];
     P.xf[j] = X[0][j];
   }
 }

@@ -81,11 +81,6 @@ int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
     set_error("antenna table too large for the split kernel");
     return SS_ERR_UNSUPPORTED;
   }
-  if (a.joint && a.ni > 4) {
-    set_error("split precision joint solve supports up to 4 interfaces; "
-              "use precision='fp64'");
-    return SS_ERR_UNSUPPORTED;
-  }
   const RefSplitConsts k = split_consts(a);
   const size_t smem = split_smem_bytes(a, p.tb);
   if (!a.joint) return split_launch_ni0(a, k, p, smem, st);
@@ -93,7 +88,8 @@ int refracted_split_launch(RefArgs &a, const Plan &p, cudaStream_t st) {
     case 1: return split_launch_ni1(a, k, p, smem, st);
     case 2: return split_launch_ni2(a, k, p, smem, st);
     case 3: return split_launch_ni3(a, k, p, smem, st);
-    default: return split_launch_ni4(a, k, p, smem, st);
+    case 4: return split_launch_ni4(a, k, p, smem, st);
+    default: return split_launch_deep(a, k, p, smem, st);
   }
 }
 

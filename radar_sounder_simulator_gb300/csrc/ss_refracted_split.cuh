@@ -409,6 +409,9 @@ template <int NI, bool EXACT, bool GRAD = false>
 __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSplitConsts &k,
                                  const TraceS &T, const double *p64,
                                  const float *q, PathS &P) {
+  // a deep stack (NI == kDeepNI) holds up to NI interfaces in its arrays
+  // and crosses a.ni of them; the other instantiations fold ni to NI
+  const int ni = NI == kDeepNI ? a.ni : NI;
   const float *nm = k.n_leg;
   P.defer = false;
   // pass 1: mean-plane chain anchors the lookups
@@ -416,7 +419,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   {
     float Pm[3] = {T.pm0[0], T.pm0[1], T.pm0[2]};
     bool safe = true;
-    for (int i = 0; i < NI; ++i) {
+    for (int i = 0; i < ni; ++i) {
       const MeanPlane32 &M = k.mean[i];
       if (i > 0)
         for (int j = 0; j < 3; ++j) Pm[j] += M.dmp[j];
@@ -433,7 +436,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
       }
       double c64[3] = {p64[0], p64[1], p64[2]};
       const double q64[3] = {q[0], q[1], q[2]};
-      for (int i = 0; i < NI; ++i)
+      for (int i = 0; i < ni; ++i)
         cell64(a.ifc[i], c64, q64, a.n_leg[i], a.n_leg[i + 1], false, c64,
                rows[i], cols[i]);
     }
@@ -441,36 +444,36 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   // local planes and exact segment bases D_0 = o_0 - p, D_k = o_k - o_k-1,
   // D_NI = q - o_NI-1
   float O[NI][3], Nn[NI][3];
-  for (int i = 0; i < NI; ++i) cell_plane32(a.ifc[i], rows[i], cols[i], O[i],
+  for (int i = 0; i < ni; ++i) cell_plane32(a.ifc[i], rows[i], cols[i], O[i],
                                             Nn[i]);
   df D[NI + 1][3];
   p_minus(T, O[0], D[0]);
   for (int j = 0; j < 3; ++j) {
     D[0][j].hi = -D[0][j].hi;
     D[0][j].lo = -D[0][j].lo;
-    for (int i = 1; i < NI; ++i) D[i][j] = df_diff(O[i][j], O[i - 1][j]);
-    D[NI][j] = df_diff(q[j], O[NI - 1][j]);
+    for (int i = 1; i < ni; ++i) D[i][j] = df_diff(O[i][j], O[i - 1][j]);
+    D[ni][j] = df_diff(q[j], O[ni - 1][j]);
   }
   float tot[3] = {0, 0, 0};
-  for (int i = 0; i <= NI; ++i)
+  for (int i = 0; i <= ni; ++i)
     for (int j = 0; j < 3; ++j) tot[j] += D[i][j].hi;
   const float scale = fmaxf(sqrtf(dot3a(tot, tot)), kTiny32);
   const float inv = 1.0f / scale;
   float Ds[NI + 1][3];
-  for (int i = 0; i <= NI; ++i)
+  for (int i = 0; i <= ni; ++i)
     for (int j = 0; j < 3; ++j) Ds[i][j] = D[i][j].hi * inv;
   // chain initialiser (25 iterations), offsets y_i from o_i (scaled)
   float Y[NI][3];
   {
     float Qrel[NI][3];  // q - o_i = sum_{j > i} D_j
     for (int j = 0; j < 3; ++j) {
-      float acc = Ds[NI][j];
-      for (int i = NI - 1; i >= 0; --i) {
+      float acc = Ds[ni][j];
+      for (int i = ni - 1; i >= 0; --i) {
         Qrel[i][j] = acc;
         acc += Ds[i][j];
       }
     }
-    for (int i = 0; i < NI; ++i) {
+    for (int i = 0; i < ni; ++i) {
       float Pr[3];
       for (int j = 0; j < 3; ++j)
         Pr[j] = i == 0 ? -Ds[0][j] : Y[i - 1][j] - Ds[i][j];
@@ -481,7 +484,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   }
   // in-plane bases and offsets
   float B[NI][3][2], ab[NI][2];
-  for (int i = 0; i < NI; ++i) {
+  for (int i = 0; i < ni; ++i) {
     const float *n = Nn[i];
     const bool use_z = fabsf(n[2]) < 0.9f;
     const float a0 = use_z ? 0.0f : 1.0f, a2 = use_z ? 1.0f : 0.0f;
@@ -500,7 +503,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   }
   // B_i^T B_{i+1}: constant over the Newton steps
   float G[NI > 1 ? NI - 1 : 1][2][2];
-  for (int i = 0; i + 1 < NI; ++i)
+  for (int i = 0; i + 1 < ni; ++i)
     for (int r = 0; r < 2; ++r)
       for (int c = 0; c < 2; ++c)
         G[i][r][c] = B[i][0][r] * B[i + 1][0][c] +
@@ -516,20 +519,20 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
                   float (&dv)[NI + 1][3], float (&pv)[NI][2],
                   float (&qv)[NI][2], float (&fv)[NI][2]) {
     float y[NI][3];
-    for (int i = 0; i < NI; ++i)
+    for (int i = 0; i < ni; ++i)
       for (int j = 0; j < 3; ++j)
         y[i][j] = B[i][j][0] * abv[i][0] + B[i][j][1] * abv[i][1];
-    for (int kk = 0; kk <= NI; ++kk) {
+    for (int kk = 0; kk <= ni; ++kk) {
       float d[3];
       for (int j = 0; j < 3; ++j)
-        d[j] = Ds[kk][j] + (kk < NI ? y[kk][j] : 0.0f) -
+        d[j] = Ds[kk][j] + (kk < ni ? y[kk][j] : 0.0f) -
                (kk > 0 ? y[kk - 1][j] : 0.0f);
       const float ss = fmaxf(sqrtf(dot3a(d, d)), kTiny32);
       sv[kk] = ss;
       const float is = 1.0f / ss;
       for (int j = 0; j < 3; ++j) dv[kk][j] = d[j] * is;
     }
-    for (int i = 0; i < NI; ++i)
+    for (int i = 0; i < ni; ++i)
       for (int c = 0; c < 2; ++c) {
         pv[i][c] = B[i][0][c] * dv[i][0] + B[i][1][c] * dv[i][1] +
                    B[i][2][c] * dv[i][2];
@@ -545,7 +548,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
     // so every block is a 2x2 from the projections (refraction_joint.py
     // :296-303 forms the same blocks through 3x3 products).
     float A[NI][2][2], Cm[NI > 1 ? NI - 1 : 1][2][2];
-    for (int i = 0; i < NI; ++i) {
+    for (int i = 0; i < ni; ++i) {
       const float sa = nm[i] / s[i], sb = nm[i + 1] / s[i + 1];
       for (int r = 0; r < 2; ++r)
         for (int c = 0; c < 2; ++c)
@@ -553,7 +556,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
                        sb * ((r == c ? 1.0f : 0.0f) - qq[i][r] * qq[i][c]) +
                        (r == c ? mu : 0.0f);
     }
-    for (int i = 0; i + 1 < NI; ++i) {
+    for (int i = 0; i + 1 < ni; ++i) {
       const float sb = nm[i + 1] / s[i + 1];
       for (int r = 0; r < 2; ++r)
         for (int c = 0; c < 2; ++c)
@@ -561,7 +564,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
     }
     // block Thomas (refraction_joint.py:218-246)
     float dinv[NI][2][2], yv[NI][2], delta[NI][2];
-    for (int i = 0; i < NI; ++i) {
+    for (int i = 0; i < ni; ++i) {
       float M[2][2] = {{A[i][0][0], A[i][0][1]}, {A[i][1][0], A[i][1][1]}};
       float rhs[2] = {-f[i][0], -f[i][1]};
       if (i > 0) {
@@ -586,9 +589,9 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
       yv[i][0] = rhs[0];
       yv[i][1] = rhs[1];
     }
-    for (int i = NI - 1; i >= 0; --i) {
+    for (int i = ni - 1; i >= 0; --i) {
       float rr[2] = {yv[i][0], yv[i][1]};
-      if (i < NI - 1)
+      if (i < ni - 1)
         for (int r = 0; r < 2; ++r)
           rr[r] -= Cm[i][r][0] * delta[i + 1][0] + Cm[i][r][1] * delta[i + 1][1];
       for (int r = 0; r < 2; ++r)
@@ -596,10 +599,10 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
     }
     // converged to float32 resolution: take the step and stop
     float dmax = 0.0f;
-    for (int i = 0; i < NI; ++i)
+    for (int i = 0; i < ni; ++i)
       dmax = fmaxf(dmax, fmaxf(fabsf(delta[i][0]), fabsf(delta[i][1])));
     if (dmax < 1e-7f) {
-      for (int i = 0; i < NI; ++i)
+      for (int i = 0; i < ni; ++i)
         for (int r = 0; r < 2; ++r) ab[i][r] += delta[i][r];
       break;
     }
@@ -611,56 +614,56 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
     // confirming Newton system is skipped too (a threshold of 3e-4 already
     // shows in the bed's phase, 3e-5 and 1e-5 do not)
     if (dmax < 1e-2f) {
-      for (int i = 0; i < NI; ++i)
+      for (int i = 0; i < ni; ++i)
         for (int r = 0; r < 2; ++r) ab[i][r] += delta[i][r];
       if (dmax < 1e-5f) break;
       continue;
     }
     float m0 = 0.0f;
-    for (int i = 0; i < NI; ++i) m0 += f[i][0] * f[i][0] + f[i][1] * f[i][1];
+    for (int i = 0; i < ni; ++i) m0 += f[i][0] * f[i][0] + f[i][1] * f[i][1];
     float lam_sel = 0.0f, lam = 1.0f;
     for (int j = 0; j < a.n_backtrack; ++j, lam *= 0.5f) {
       float cand[NI][2], sc[NI + 1], dc[NI + 1][3], pc[NI][2], qc[NI][2],
           fc[NI][2];
-      for (int i = 0; i < NI; ++i)
+      for (int i = 0; i < ni; ++i)
         for (int r = 0; r < 2; ++r) cand[i][r] = ab[i][r] + lam * delta[i][r];
       geom(cand, sc, dc, pc, qc, fc);
       float mc = 0.0f;
-      for (int i = 0; i < NI; ++i) mc += fc[i][0] * fc[i][0] + fc[i][1] * fc[i][1];
+      for (int i = 0; i < ni; ++i) mc += fc[i][0] * fc[i][0] + fc[i][1] * fc[i][1];
       if (mc < m0) {
         lam_sel = lam;
         break;
       }
     }
-    for (int i = 0; i < NI; ++i)
+    for (int i = 0; i < ni; ++i)
       for (int r = 0; r < 2; ++r) ab[i][r] += lam_sel * delta[i][r];
   }
   geom(ab, s, dh, pp, qq, f);
   // crossings in metres from their facet centres; exact segment lengths
   float Ym[NI][3];
-  for (int i = 0; i < NI; ++i)
+  for (int i = 0; i < ni; ++i)
     for (int j = 0; j < 3; ++j)
       Ym[i][j] = scale * (B[i][j][0] * ab[i][0] + B[i][j][1] * ab[i][1]);
   df S[NI + 1];
   df seg_last[3];
-  for (int kk = 0; kk <= NI; ++kk) {
+  for (int kk = 0; kk <= ni; ++kk) {
     df v[3];
     for (int j = 0; j < 3; ++j) {
       v[j] = D[kk][j];
-      if (kk < NI) v[j] = df_add_f(v[j], Ym[kk][j]);
+      if (kk < ni) v[j] = df_add_f(v[j], Ym[kk][j]);
       if (kk > 0) v[j] = df_add_f(v[j], -Ym[kk - 1][j]);
     }
     S[kk] = df_norm3(v[0], v[1], v[2]);
     if (kk == 0)
       for (int j = 0; j < 3; ++j) P.d0[j] = v[j].hi;
-    if (kk == NI)
+    if (kk == ni)
       for (int j = 0; j < 3; ++j) seg_last[j] = v[j];
   }
   // validity: residual, straddling, evanescence (refraction_joint:143-176)
   float residual = 0.0f;
   bool sides = true, evan = false;
   float cinc[NI], cout_[NI];
-  for (int i = 0; i < NI; ++i) {
+  for (int i = 0; i < ni; ++i) {
     const float *n = Nn[i];
     const float ct1 = dot3a(n, dh[i]), ct2 = dot3a(n, dh[i + 1]);
     float t1[3], t2[3], dG[3];
@@ -688,7 +691,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   // crossing i onto the stored plane changes its two legs by hp c_in and
   // -hp c_out, hp its height over that plane towards the upper point.
   float dopl = 0.0f;
-  for (int i = 0; i < NI; ++i) {
+  for (int i = 0; i < ni; ++i) {
     const float *g =
         a.ifc[i].table + ((size_t)rows[i] * a.ifc[i].nx + cols[i]) * 6;
     const float tn[3] = {g[3], g[4], g[5]};
@@ -698,11 +701,11 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   }
   // radiometry sums and optical path (multilayer.py:436-457)
   float c_inc[NI];
-  for (int i = 0; i < NI; ++i) c_inc[i] = fmaxf(cinc[i], (float)kCMin);
+  for (int i = 0; i < ni; ++i) c_inc[i] = fmaxf(cinc[i], (float)kCMin);
   const float c_surf = c_inc[a.k_pad];
   float tau2 = 1.0f, loss = 0.0f, sperp = 0.0f, spar = 0.0f, dloss = 0.0f;
   df opl = df_make(0.0f, 0.0f);
-  for (int i = 0; i < NI; ++i) {
+  for (int i = 0; i < ni; ++i) {
     const float g = fresnel_gamma32(k.eps_leg[i], k.eps_leg[i + 1], c_inc[i]);
     tau2 *= (1.0f - g * g);
     if (a.rough_cross) {
@@ -725,9 +728,9 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   P.sum_perp = sperp;
   P.sum_par = spar;
   P.c0 = c_surf;
-  P.c_last = fmaxf(cout_[NI - 1], (float)kCMin);
-  P.s_last = S[NI];
-  const float is = 1.0f / fmaxf(S[NI].hi, 1e-30f);
+  P.c_last = fmaxf(cout_[ni - 1], (float)kCMin);
+  P.s_last = S[ni];
+  const float is = 1.0f / fmaxf(S[ni].hi, 1e-30f);
   for (int j = 0; j < 3; ++j) P.rh[j] = -seg_last[j].hi * is;
 }
 
@@ -1414,5 +1417,9 @@ int split_launch_ni3(RefArgs &a, const RefSplitConsts &k, const Plan &p,
                      size_t smem, cudaStream_t st);
 int split_launch_ni4(RefArgs &a, const RefSplitConsts &k, const Plan &p,
                      size_t smem, cudaStream_t st);
+// Joint solve through 5..SS_MAX_IFACE interfaces: one instantiation whose
+// arrays hold SS_MAX_IFACE interfaces (in local memory).
+int split_launch_deep(RefArgs &a, const RefSplitConsts &k, const Plan &p,
+                      size_t smem, cudaStream_t st);
 
 }  // namespace ss

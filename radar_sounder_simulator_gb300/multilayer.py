@@ -219,8 +219,8 @@ def prepare_refracted(positions, u_ct, target, crossed, eps_leg, att_leg, *,
         if sig_c is not None:
             sig_c = np.concatenate([np.zeros(k_pad), sig_c])
     ni = k_pad + len(crossed)
-    if not 1 <= ni <= 8:
-        raise ValueError(f"{ni} crossed interfaces; the kernel takes 1..8")
+    if not 1 <= ni <= 40:
+        raise ValueError(f"{ni} crossed interfaces; the kernel takes 1..40")
     if len(n_leg) < ni + 1 or (joint and len(n_leg) != ni + 1):
         raise ValueError("eps_leg/att_leg need len(crossed) + 1 entries")
     ifaces += [grid_consts_device(f, device) for f in crossed]

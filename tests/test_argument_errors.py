@@ -98,7 +98,7 @@ def test_refracted_stack_errors():
                    refraction="joint", pad_to=1)
     with pytest.raises(ValueError, match="len\\(crossed\\) \\+ 1"):
         _refracted(eps=(1.0,))
-    with pytest.raises(ValueError, match="takes 1..8"):
+    with pytest.raises(ValueError, match="takes 1..40"):
         _refracted(crossed=(), eps=(1.0,))
 
 

@@ -70,17 +70,16 @@ def test_padding_is_exact_noop(precision, tol):
     tgt, crossed, eps, kw = _firn_case()
     base, _ = _run(tgt, crossed, eps, kw, precision, refraction="joint")
     assert np.abs(base).max() > 0
-    # the split form's joint solve is built for up to four crossings; a
-    # larger padded stack is refused, never truncated
-    for pad in (4, 8) if precision == "fp64" else (4,):
+    # 4 crossings run the register-resident solve, 8 and 16 the deep-stack
+    # instantiation (its arrays in local memory) in the split form
+    for pad in (4, 8, 16):
         padded, _ = _run(tgt, crossed, eps, kw, precision,
                          refraction="joint", pad_to=pad)
         d = np.abs(padded - base).max() / np.abs(base).max()
         assert d < tol, (pad, d)
-    if precision == "split":
-        with pytest.raises(ValueError):
-            _run(tgt, crossed, eps, kw, precision, refraction="joint",
-                 pad_to=8)
+    with pytest.raises(ValueError):
+        _run(tgt, crossed, eps, kw, precision, refraction="joint",
+             pad_to=41)
 
 
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-9), ("split", 1e-5)])
