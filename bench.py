@@ -60,6 +60,11 @@ def parse():
                     help="secondary workloads measured after the headline "
                          "(comma list, or 'none')")
     ap.add_argument("--batch-instances", type=int, default=96)
+    ap.add_argument("--kernel-only", default=None,
+                    choices=["surface", "h1", "h2", "bed"],
+                    help="run only this target of the multilayer scene "
+                         "(warm-up + steps launches, for profiling) and "
+                         "print its mean time")
     ap.add_argument("--fp64-traces", type=int, default=256,
                     help="traces of the float64-form step (its rate is per "
                          "pair; the error check covers these traces)")
@@ -340,6 +345,9 @@ def main():
     pairs_step = sum(len(f.centers) for f in cfg.layers) * len(cfg.pos)
 
     plans = build_plans(cfg, "split", device)
+    if args.kernel_only:
+        run_kernel_only(args, plans, device)
+        return
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=device)
     stream = torch.cuda.current_stream(device)
 
@@ -452,9 +460,32 @@ def main():
                                            "bed_joint"], per_kernel)),
                 "gpu_launches": launches, "roofline": roof,
                 "clocks": clk.summary(), "cpu_baseline": cpu, "rows": rows}
+        # last key, so a reader that keeps only the line's tail still has
+        # every row's rate and split-vs-FP64 error
+        line["summary"] = summarize(line)
         print(json.dumps(line), flush=True)
     if ws > 1:
         dist.destroy_process_group()
+
+
+def run_kernel_only(args, plans, device):
+    """One target's plan alone (main pass, fix-up, reduce): warm-up and
+    timed launches, mean event time printed (the profiling entry point)."""
+    import torch
+    p = plans[["surface", "h1", "h2", "bed"].index(args.kernel_only)]
+    for _ in range(args.warmup):
+        p.run()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        p.run()
+    e1.record()
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel_only": args.kernel_only,
+                      "ms": e0.elapsed_time(e1) / max(args.steps, 1)}),
+          flush=True)
 
 
 # --------------------------------------------------------------------------
@@ -692,15 +723,10 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32, cpu_seconds=0.0):
     bands = {}
     total_ms, total_pairs = 0.0, 0
     for f0 in cfg.bands:
-        bw = cfg.frac_bw * f0
-        dt = 1.0 / (2.0 * bw)
-        k0 = 2 * np.pi * f0 / c
-        n_s = int(np.ceil(2 * (1000.0 * np.sqrt(3.15) + 3000.0) / c / dt))
-        t0 = scenes.window(cfg.pos, s.centers, n_samples=n_s, dt=dt)
+        bd = scenes.config3_band(cfg, f0)
+        bw, dt, k0, n_s, t0 = bd["bw"], bd["dt"], bd["k0"], bd["n_s"], bd["t0"]
+        nt_s, nt_b = bd["nt_s"], bd["nt_b"]
         rs, rb = cfg.rough["surface"], cfg.rough["bed"]
-        nt_s = scenes.n_terms_for((2 * k0 * rs["sigma"].max()) ** 2)
-        nt_b = scenes.n_terms_for((2 * k0 * np.sqrt(3.15) *
-                                   np.quantile(rb["sigma"], 0.999)) ** 2)
 
         def plans(pos, uct, nts=nt_s, ntb=nt_b):
             ps = prepare_coherent(
@@ -911,9 +937,107 @@ def row_cfg4(device, n_inst, flush, peaks, cpu_seconds=0.0):
                 lambda: cfg4_cpu_baseline(cpu_seconds), cpu_seconds)}
 
 
-def row_cfg5(device, flush):
+def cfg5_fd_subset(cfg, device, n_traces=32, n_check=16):
+    """Adjoint of the split form against central differences of the FP64
+    GPU forward on the central ``n_traces`` traces of the configuration:
+    ``n_check`` seeded facets per kind among the most-illuminated tenth,
+    relative step 2^-13. Returns the largest per-entry relative error per
+    kind (absolute floor 1e-5 of the kind's largest checked gradient)."""
+    import torch
+    from radar_sounder_simulator_gb300.adjoint import (WindowPowerModel,
+                                                       db_misfit)
+    mid = len(cfg.pos) // 2
+    sl = slice(mid - n_traces // 2, mid + n_traces // 2)
+
+    def model(prec):
+        return WindowPowerModel(
+            cfg.pos[sl], cfg.uct[sl], cfg.bed, [cfg.surface], cfg.eps,
+            [0.0, cfg.alpha], t0=cfg.t0, dt=cfg.dt, n_samples=cfg.n_samples,
+            c=cfg.c, k0=cfg.k0, window=cfg.window, alpha_legs=(1,),
+            corr_length=cfg.corr, phasors=cfg.phasors, n_terms=cfg.n_terms,
+            precision=prec, device=device)
+    m32, m64 = model("split"), model("fp64")
+    dev = m32.device
+
+    def t(v):
+        return torch.tensor(v, dtype=torch.float64, device=dev)
+    with torch.no_grad():
+        P_hat = m64.power(t(cfg.R_hat), t(cfg.sig_hat), t(cfg.alpha + 1.0))
+    R = t(cfg.R).requires_grad_(True)
+    sg = t(cfg.sig).requires_grad_(True)
+    a = t(cfg.alpha).requires_grad_(True)
+    db_misfit(m32.power(R, sg, a), P_hat).backward()
+
+    def loss(Rv, sv, av):
+        with torch.no_grad():
+            return float(db_misfit(m64.power(Rv, sv, av), P_hat))
+    rng = np.random.default_rng(55)
+    h = 2.0 ** -13
+    out = {}
+    for name, g, base in (("reflectivity_db", R.grad, cfg.R),
+                          ("rms_height", sg.grad, cfg.sig)):
+        gm = g.abs().cpu().numpy()
+        top = np.argsort(gm)[-max(len(gm) // 10, n_check):]
+        idx = rng.choice(top, size=n_check, replace=False)
+        fd = []
+        for i in idx:
+            vp, vm = base.copy(), base.copy()
+            d = h * abs(base[i])
+            vp[i] += d
+            vm[i] -= d
+            if name == "reflectivity_db":
+                fd.append((loss(t(vp), t(cfg.sig), t(cfg.alpha)) -
+                           loss(t(vm), t(cfg.sig), t(cfg.alpha))) / (2 * d))
+            else:
+                fd.append((loss(t(cfg.R), t(vp), t(cfg.alpha)) -
+                           loss(t(cfg.R), t(vm), t(cfg.alpha))) / (2 * d))
+        fd = np.array(fd)
+        got = g.cpu().numpy()[idx]
+        floor = 1e-5 * np.abs(fd).max()
+        out[name] = float((np.abs(got - fd) / (np.abs(fd) + floor)).max())
+    da = h * cfg.alpha
+    fda = (loss(t(cfg.R), t(cfg.sig), t(cfg.alpha + da)) -
+           loss(t(cfg.R), t(cfg.sig), t(cfg.alpha - da))) / (2 * da)
+    out["alpha"] = float(abs(float(a.grad) - fda) / abs(fda))
+    out.update(traces=n_traces, params_per_kind=n_check,
+               referee="central differences of the FP64 GPU forward, "
+                       "relative step 2^-13")
+    return out
+
+
+def cfg5_cpu_baseline(cfg, seconds):
+    """The float64 NumPy oracle forward of the bed on one host core, trace
+    by trace from the middle of the track (at least one trace). There is
+    no CPU adjoint: a CPU gradient by central differences would cost two
+    such forwards per parameter."""
+    from oracle import refracted as oref
+    T = len(cfg.pos)
+    mid = T // 2
+    t0 = time.perf_counter()
+    done = 0
+    while mid + done < T and (done == 0 or
+                              time.perf_counter() - t0 < seconds):
+        sl = slice(mid + done, mid + done + 1)
+        oref.refracted_cluttergram(
+            cfg.pos[sl], cfg.uct[sl], cfg.bed, [cfg.surface], cfg.eps,
+            [0.0, cfg.alpha], mode="coherent", t0=cfg.t0, dt=cfg.dt,
+            n_samples=cfg.n_samples, c=cfg.c, gamma=10.0 ** (cfg.R / 20.0),
+            k0=cfg.k0, roughness=(cfg.sig, cfg.corr, cfg.phasors,
+                                  cfg.n_terms, "exponential"),
+            d_phi_area=True, taper_s=0.05, refraction="sequential")
+        done += 1
+    el = time.perf_counter() - t0
+    n = len(cfg.bed.centers)
+    return {"value": done * n / el, "unit": "contribs/s", "cores": 1,
+            "kind": "port",
+            "sample": f"{done} traces x {n} bed facets, float64 NumPy "
+                      f"oracle forward (no CPU adjoint exists), {el:.1f} s"}
+
+
+def row_cfg5(device, flush, peaks, cpu_seconds=0.0):
     """Adjoint: forward bed power and hand-written backward of the dB
-    misfit, 512^2 bed facets x 1024 traces."""
+    misfit, 512^2 bed facets x 1024 traces; a finite-difference subset on
+    the central traces; roofline of the backward pass."""
     import torch
     from radar_sounder_simulator_gb300 import scenes
     from radar_sounder_simulator_gb300.adjoint import (WindowPowerModel,
@@ -948,10 +1072,30 @@ def row_cfg5(device, flush):
     e1.record()
     torch.cuda.synchronize()
     ts["backward_ms"] = e0.elapsed_time(e1)
-    pairs = len(cfg.bed.centers) * len(cfg.pos)
+    T, n = len(cfg.pos), len(cfg.bed.centers)
+    pairs = n * T
+    # canonical backward work per pair: the sequential refracted pair, taper
+    # and rough overhead, 12 FLOP per series term (the series and its
+    # x-derivative sum) over each facet's own term count, and 24 for the
+    # three gradient accumulations
+    x = (2.0 * cfg.k0 * np.sqrt(cfg.eps[1]) * np.asarray(cfg.sig)) ** 2
+    terms = np.clip(np.ceil(x + 6.0 * np.sqrt(x) + 5.0), 10, cfg.n_terms)
+    flop = T * np.sum(pair_flops(1, False) + 6 + 20 + 12 * terms + 24)
+    roof = _roof(flop, ts["backward_ms"], peaks["fp32"], "fp32",
+                 float(flop / pairs),
+                 "backward pass (adjoint + fix-up), canonical per-pair "
+                 "FLOP: sequential refracted pair 865, taper 6, rough 20, "
+                 "12 per series term, 24 accumulation")
+    try:
+        fdsub = cfg5_fd_subset(cfg, device)
+    except Exception as exc:  # reported, not hidden
+        fdsub = {"error": f"{type(exc).__name__}: {exc}"}
     return {"workload": "adjoint_bed_512sq_1024tr", "unit": "contribs/s",
             "value": pairs / (ts["backward_ms"] * 1e-3), **ts,
-            "n_terms": cfg.n_terms,
+            "n_terms": cfg.n_terms, "roofline": roof,
+            "fd_subset_max_rel_err": fdsub,
+            "cpu_baseline": _cpu_or_error(
+                lambda: cfg5_cpu_baseline(cfg, cpu_seconds), cpu_seconds),
             "grad_norms": {"reflectivity_db": float(R.grad.norm()),
                            "rms_height": float(sg.grad.norm()),
                            "alpha": float(a.grad)}}
@@ -1164,7 +1308,8 @@ def run_rows(args, device, peak32):
                                     min(args.cpu_seconds, 5.0)),
            "cfg4": lambda: row_cfg4(device, args.batch_instances, flush,
                                     peaks, min(args.cpu_seconds, 5.0)),
-           "cfg5": lambda: row_cfg5(device, flush),
+           "cfg5": lambda: row_cfg5(device, flush, peaks,
+                                    min(args.cpu_seconds, 5.0)),
            "incoh": lambda: row_incoh(device, flush, peaks),
            "focus": lambda: row_focus(device, flush, peaks),
            "scene": lambda: row_scene(device, flush),
@@ -1178,6 +1323,46 @@ def run_rows(args, device, peak32):
         rows[name]["wall_s"] = time.perf_counter() - t0
         torch.cuda.empty_cache()
     return rows
+
+
+def _short(err):
+    if not isinstance(err, dict) or "rel_l2" not in err:
+        return err
+    return [float(f"{err['rel_l2']:.2e}"), float(f"{err['phase_rad']:.2e}"),
+            float(f"{err['power_db']:.2e}")]
+
+
+def summarize(line):
+    """Compact per-row rates and split-vs-FP64 errors ([rel L2, rad, dB])
+    of a bench line."""
+    out = {"headline": {"value": float(f"{line['value']:.4g}"),
+                        "ms": round(line["ms_per_step"], 2),
+                        "err": _short(line.get("error_vs_fp64")),
+                        "frac": round(line["roofline"]["frac"], 3)}}
+    rows = line.get("rows") or {}
+    for name, r in rows.items():
+        if not isinstance(r, dict) or name == "peaks_tflops":
+            continue
+        if "error" in r:
+            out[name] = {"error": r["error"][:120]}
+            continue
+        e = {"value": float(f"{r.get('value', 0.0):.4g}")}
+        if "error_vs_fp64" in r:
+            e["err"] = _short(r["error_vs_fp64"])
+        if "roofline" in r and isinstance(r["roofline"], dict):
+            e["frac"] = round(r["roofline"].get("frac", 0.0), 3)
+        if "fd_subset_max_rel_err" in r:
+            fd = r["fd_subset_max_rel_err"]
+            e["fd"] = ({k: float(f"{v:.2e}") for k, v in fd.items()
+                        if isinstance(v, float)} if "error" not in fd
+                       else fd["error"][:80])
+        if name == "cfg3":
+            e["bands"] = {b: {"ms": round(v["ms"], 1),
+                              "err": _short(v.get("error_vs_fp64")),
+                              "frac": round(v["roofline"]["frac"], 3)}
+                          for b, v in r["bands"].items()}
+        out[name] = e
+    return out
 
 
 def split_error(outs, outs64):

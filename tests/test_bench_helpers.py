@@ -97,3 +97,27 @@ def test_sweep_cpu_baseline_one_slice():
     cb = bench.cfg4_cpu_baseline(0.0)                  # one 8-trace slice
     assert cb["value"] > 0 and cb["unit"] == "contribs/s"
     assert cb["sample"].startswith("8 traces x ")
+
+
+def test_summary_is_compact_and_carries_row_errors():
+    import json
+    import bench
+    err = {"rel_l2": 1.234e-6, "phase_rad": 2.5e-4, "power_db": 3.1e-3}
+    line = {"value": 8.0e9, "ms_per_step": 130.123, "error_vs_fp64": err,
+            "roofline": {"frac": 0.5123},
+            "rows": {"peaks_tflops": {"fp32": 78.0},
+                     "cfg1": {"value": 1e10, "error_vs_fp64": err,
+                              "roofline": {"frac": 0.1}},
+                     "cfg3": {"value": 1e10, "bands": {
+                         "450MHz": {"ms": 123.4, "error_vs_fp64": err,
+                                    "roofline": {"frac": 0.2}}}},
+                     "cfg5": {"value": 4e9, "fd_subset_max_rel_err": {
+                         "reflectivity_db": 1e-5, "traces": 32}},
+                     "broken": {"error": "RuntimeError: x" * 50}}}
+    s = bench.summarize(line)
+    assert s["headline"]["err"] == [1.23e-6, 2.5e-4, 3.1e-3]
+    assert s["cfg3"]["bands"]["450MHz"]["err"][1] == 2.5e-4
+    assert s["cfg5"]["fd"] == {"reflectivity_db": 1e-5}
+    assert "peaks_tflops" not in s
+    assert len(s["broken"]["error"]) <= 120
+    assert len(json.dumps(s)) < 1200
