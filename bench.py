@@ -829,9 +829,14 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32, cpu_seconds=0.0):
         total_ms += ms
         total_pairs += pairs
         del ps, pb
+    try:
+        batched = cfg3_batched(cfg, device, flush, total_pairs,
+                               sum(b["kernel_ms"] for b in bands.values()))
+    except Exception as exc:  # reported, not hidden
+        batched = {"error": f"{type(exc).__name__}: {exc}"}
     return {"workload": "rough_surface_bed_512sq_25m_2048tr_4bands",
             "unit": "contribs/s", "value": total_pairs / (total_ms * 1e-3),
-            "ms_per_step": total_ms, "bands": bands,
+            "ms_per_step": total_ms, "bands": bands, "batched": batched,
             "roofline_note": "per band: the slower of the FP32 and MUFU "
                              "pipes at the canonical per-pair counts (FP32 "
                              "47 or the sequential refracted pair + 6 taper "
@@ -839,6 +844,57 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32, cpu_seconds=0.0):
                              "3 + 2 per term; terms per facet from its "
                              "sigma) over the kernels' event time, against "
                              "the FMA and MUFU rates measured in this run"}
+
+
+def cfg3_batched(cfg, device, flush, pairs, per_call_ms):
+    """The roughness configuration's eight (target, band) jobs as one
+    persistent surface batch and one persistent refracted batch, captured
+    in one CUDA graph and replayed once per step; every job's field is
+    checked against its own per-call result."""
+    import torch
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.batch import (BatchGraph,
+                                                     CoherentBatch,
+                                                     RefractedBatch)
+    from radar_sounder_simulator_gb300.coherent import prepare_coherent
+    from radar_sounder_simulator_gb300.multilayer import prepare_refracted
+    s, b = cfg.surface, cfg.bed
+    rs, rb = cfg.rough["surface"], cfg.rough["bed"]
+    surf, bed = [], []
+    for f0 in cfg.bands:
+        bd = scenes.config3_band(cfg, f0)
+        common = dict(t0=bd["t0"], dt=bd["dt"], n_samples=bd["n_s"],
+                      c=cfg.c, d_phi_area=True, taper_s=0.05,
+                      precision="split", device=device)
+        surf.append(prepare_coherent(
+            cfg.pos, cfg.uct, s.centers, s.normals, s.areas, s.e1, s.e2,
+            k=bd["k0"], gamma=cfg.gamma_surface,
+            roughness=(rs["sigma"], rs["corr"], rs["phasors"], bd["nt_s"],
+                       "exponential"), **common))
+        bed.append(prepare_refracted(
+            cfg.pos, cfg.uct, b, [s], cfg.eps, cfg.att, mode="coherent",
+            gamma=cfg.gamma_bed, k0=bd["k0"],
+            roughness=(rb["sigma"], rb["corr"], rb["phasors"], bd["nt_b"],
+                       "exponential"), refraction="sequential", **common))
+    cb, rbt = CoherentBatch(surf), RefractedBatch(bed)
+    graph = BatchGraph([cb.run, rbt.run], device)
+    graph.capture()
+    ms = _events_ms(graph.replay, 3, flush)
+    torch.cuda.synchronize()
+    worst = 0.0
+    for plans, outs in ((surf, cb.outputs), (bed, rbt.outputs)):
+        for p, (field, _) in zip(plans, outs):
+            one = p.run()[0]
+            a, r = _complex(field), _complex(one)
+            worst = max(worst, float(torch.linalg.vector_norm(a - r) /
+                                     torch.linalg.vector_norm(r)))
+    out = {"jobs": len(surf) + len(bed), "graph_replays_per_step": 1,
+           "kernel_launches": cb.kernel_launches() + rbt.kernel_launches(),
+           "ms": ms, "contribs_per_s": pairs / (ms * 1e-3),
+           "per_call_kernel_ms": per_call_ms,
+           "max_rel_l2_vs_per_call": worst}
+    del graph, cb, rbt, surf, bed
+    return out
 
 
 def cfg4_cpu_baseline(seconds):
@@ -1361,6 +1417,13 @@ def summarize(line):
                               "err": _short(v.get("error_vs_fp64")),
                               "frac": round(v["roofline"]["frac"], 3)}
                           for b, v in r["bands"].items()}
+            bt = r.get("batched") or {}
+            e["batched"] = ({"ms": round(bt["ms"], 1),
+                             "per_call_ms": round(bt["per_call_kernel_ms"],
+                                                  1),
+                             "rel_l2": float(
+                                 f"{bt['max_rel_l2_vs_per_call']:.2e}")}
+                            if "ms" in bt else bt.get("error", "")[:80])
         out[name] = e
     return out
 
