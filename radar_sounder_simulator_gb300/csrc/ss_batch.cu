@@ -107,9 +107,11 @@ static int batch_layout(const ss_coherent_job *jobs, int n_jobs,
     off += align256((size_t)J.n_chunks * a.T * a.n_seg * elt);
     a.part_drop = reinterpret_cast<double *>(off);
     off += align256((size_t)J.n_chunks * a.T * sizeof(double));
-    const size_t lg = a.rough_kind ? (size_t)(a.n_terms + 1) *
-                                         (a.precision == SS_PREC_FP64 ? 8 : 4)
-                                   : 0;
+    // the FP64 kernel stages log-factorials of the series; the split kernel
+    // anchors its Poisson weights without a table
+    const size_t lg = a.rough_kind && a.precision == SS_PREC_FP64
+                          ? (size_t)(a.n_terms + 1) * 8
+                          : 0;
     L.smem = std::max(L.smem, (size_t)a.tb * a.n_seg * elt + lg);
   }
   L.n_items = item;

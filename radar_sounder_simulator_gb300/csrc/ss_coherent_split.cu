@@ -1,20 +1,37 @@
 // Split-precision surface coherent kernel.
 //
 // Same decomposition as the FP64 form (ss_coherent.cu). Per pair, only three
-// quantities need more than float32:
-//   * the slant range r (20 km at 1 mm f32 ulp; 1e-3 rad at 450 MHz needs
-//     ~50 um): carried as double-float from a double-float platform position
-//     and the float32 facet centroid (exact), one rsqrt + Newton correction;
-//   * the carrier phase 2 k r: a double-float product reduced modulo 2 pi
-//     with a two-constant Cody-Waite step (exact first step by construction),
-//     then MUFU sin/cos on an argument in [-pi, pi];
-//   * the fast-time bin floor((2r/c - t0)/dt): evaluated from the
-//     double-float range; a pair whose fractional bin position lies within
-//     1e-6 of an edge is re-binned with the float64 round-to-nearest chain of
-//     the oracle, so bins are bit-identical to the float64 form.
+// quantities need more than float32: the slant range r (20 km at 1 mm f32
+// ulp; 1e-3 rad at 450 MHz needs ~50 um), the carrier phase 2 k r and the
+// fast-time bin floor((2r/c - t0)/dt). They are formed in two stages.
+//
+//   * Once per facet and trace block (a CTA's `tb` neighbouring traces): the
+//     range r_c to the block's middle trace as a double-float (exact
+//     difference of the double-float platform and the float32 centroid,
+//     exact squares, rsqrt + Newton), its phase 2 k r_c reduced modulo 2 pi
+//     (double-float product, two-constant Cody-Waite whose first step is
+//     exact), its bin position split into an integer and a fraction, and the
+//     products of q = p_c - c with the facet's normal and edge vectors.
+//   * Per trace t of the block, with w = p_t - p_c (a few trace spacings):
+//     r_t^2 - r_c^2 = 2 q.w + |w|^2 = N, so r_t - r_c = N / (r_c + r_t) in
+//     float32. Its relative error is below 6e-7 (three roundings of the
+//     2 q.w sum against D = 2r, the rsqrt of r_t and the division), so the
+//     absolute error is below 6e-7 |w|: 1.5e-5 m for a 25 m spacing, 2.8e-4
+//     rad of phase at 450 MHz in the worst case and ~5e-5 rad typically.
+//     The middle trace has w = 0 and its pairs are exact to the reference's
+//     double-float.
+//
+// The bin of a pair within 4e-6 + 1e-6 |w|_max A bins of an edge (A = 2 /
+// (c dt), bins per metre) is decided by the float64 round-to-nearest chain
+// of the oracle, so bins are bit-identical to the float64 form: the band
+// is twice the largest error of the float32 bin position. A block whose
+// traces lie more than 64 m from its middle trace (sparse or crooked
+// tracks) takes a reference per trace instead (w = 0 for every pair).
+//
 // Everything else (incidence, sincs, taper, antenna gain, roughness series)
-// runs in float32; histograms accumulate float32 per CTA chunk and chunks are
-// summed in float64 by the reduce kernel.
+// runs in float32 from q + w and the facet's per-block products;
+// histograms accumulate float32 per CTA chunk and chunks are summed in
+// float64 by the reduce kernel.
 #include <algorithm>
 
 #include "ss_coherent.cuh"
@@ -23,22 +40,8 @@
 
 namespace ss {
 
-// (dh + dl) . e for a double-float vector d and float e: exact products
-// (two_prod), compensated sum, rounded once to float.
-__device__ __forceinline__ float dot_df(float xh, float xl, float yh, float yl,
-                                        float zh, float zl, float ex, float ey,
-                                        float ez) {
-  float px, qx, py, qy, pz, qz, s, e1, e2;
-  two_prod(xh, ex, px, qx);
-  two_prod(yh, ey, py, qy);
-  two_prod(zh, ez, pz, qz);
-  two_sum(px, py, s, e1);
-  two_sum(s, pz, s, e2);
-  const float lo = (e1 + e2) + (qx + qy + qz) +
-                   __fmaf_rn(xl, ex, __fmaf_rn(yl, ey, zl * ez));
-  return s + lo;
-}
-
+// Widest trace block (largest |p_t - p_c|, metres) served by one reference.
+constexpr float kWideBlock = 64.0f;
 
 // One CTA's work item: facet chunk `chunk` of trace block `group`. Shared
 // by the one-call kernel (item = block index) and the batched persistent
@@ -49,17 +52,20 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
                                                    int chunk, int group,
                                                    unsigned char *smem_raw) {
   float2 *hist = reinterpret_cast<float2 *>(smem_raw);
-  float *lg = reinterpret_cast<float *>(hist + (size_t)a.tb * a.n_seg);
   __shared__ float s_ph[SS_MAX_TB][3], s_pl[SS_MAX_TB][3];
   __shared__ double s_p64[SS_MAX_TB][3];
+  __shared__ float4 s_w[SS_MAX_TB];   // p_t - p_c (hi), |p_t - p_c|^2
+  __shared__ float4 s_wl[SS_MAX_TB];  // p_t - p_c (lo), |p_t - p_c|
   __shared__ float s_u[SS_MAX_TB][3];
   __shared__ float s_pv[SS_MAX_TB][6];
-  __shared__ int s_lo[SS_MAX_TB], s_hi[SS_MAX_TB];
+  __shared__ int2 s_win[SS_MAX_TB];
   __shared__ float s_drop[SS_MAX_TB];
   __shared__ float s_pat[SS_PAT_MAX];
   __shared__ float s_fad[SS_FAD_N];
   __shared__ int s_rng[2];
   __shared__ int s_next;
+  __shared__ int s_ref;      // the block's reference trace; -1: per trace
+  __shared__ float s_guard;  // bin-edge band of the differential form
 
   const int t_base = group * a.tb;
   const int nt = min(a.tb, a.T - t_base);
@@ -69,6 +75,8 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
 
   if (tid < nt) {
     const int t = t_base + tid;
+    const int tc = t_base + nt / 2;
+    double w[3], w2 = 0.0;
     for (int j = 0; j < 3; ++j) {
       const double pj = a.pos[3 * t + j];
       const df v = df_from_double(pj);
@@ -76,14 +84,19 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       s_pl[tid][j] = v.lo;
       s_p64[tid][j] = pj;
       s_u[tid][j] = a.uct ? (float)a.uct[3 * t + j] : 0.0f;
+      w[j] = pj - a.pos[3 * tc + j];
+      w2 += w[j] * w[j];
     }
+    const float wx = (float)w[0], wy = (float)w[1], wz = (float)w[2];
+    s_w[tid] = make_float4(wx, wy, wz, (float)w2);
+    s_wl[tid] = make_float4((float)(w[0] - wx), (float)(w[1] - wy),
+                            (float)(w[2] - wz), (float)sqrt(w2));
     for (int j = 0; j < 6; ++j)
       s_pv[tid][j] =
           (a.pv && j < a.pv_len) ? (float)a.pv[a.pv_len * t + j] : 0.0f;
     long lo = (long)a.off[t] * a.bs;
     long hi = min((long)(a.off[t] + a.n_win) * a.bs, (long)a.N);
-    s_lo[tid] = (int)min(lo, (long)a.N);
-    s_hi[tid] = (int)hi;
+    s_win[tid] = make_int2((int)min(lo, (long)a.N), (int)hi);
     s_drop[tid] = 0.0f;
   }
   for (int j = tid; j < pa_len; j += blockDim.x) s_pat[j] = (float)a.pa[j];
@@ -93,28 +106,33 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
     s_fad[tid] = (float)a.fad.a[tid];
   for (int j = tid; j < a.tb * a.n_seg; j += blockDim.x)
     hist[j] = make_float2(0.0f, 0.0f);
-  if (ROUGH != SS_ROUGH_NONE)
-    for (int m = tid; m <= a.n_terms; m += blockDim.x)
-      lg[m] = (float)lgamma((double)m + 1.0);
   __syncthreads();
   if (tid == 0) {
-    int lo = s_lo[0], hi = s_hi[0];
+    int lo = s_win[0].x, hi = s_win[0].y;
+    float wmax = s_wl[0].w;
     for (int j = 1; j < nt; ++j) {
-      lo = min(lo, s_lo[j]);
-      hi = max(hi, s_hi[j]);
+      lo = min(lo, s_win[j].x);
+      hi = max(hi, s_win[j].y);
+      wmax = fmaxf(wmax, s_wl[j].w);
     }
     long len = max(hi - lo, 0);
     s_rng[0] = lo + (int)(len * chunk / a.n_chunks);
     s_rng[1] = lo + (int)(len * (chunk + 1) / a.n_chunks);
     s_next = s_rng[0];
+    const bool one_ref = wmax <= kWideBlock;
+    s_ref = one_ref ? nt / 2 : -1;
+    s_guard = one_ref ? 4e-6f + 1e-6f * wmax * k.Ah : 1e-6f;
   }
   __syncthreads();
 
   const float nsf = (float)a.n_samples;
+  const int ref = s_ref;
+  const float guard = s_guard;
   // lane l meets the block's traces starting at trace l mod nt, so the 32
   // neighbouring facets of a warp -- often in one bin -- spread their
   // histogram atomics over the block's traces; dropped power collects per
-  // thread and trace and reaches shared memory once per trace at the end
+  // thread and step (L1-resident local memory) and reaches shared memory
+  // once per trace at the end
   const int rot = (tid & 31) % max(nt, 1);
   float dropl[SS_MAX_TB];
 #pragma unroll
@@ -136,6 +154,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
     const float e2x = a.F.e2x[i], e2y = a.F.e2y[i], e2z = a.F.e2z[i];
     const float area = a.F.area[i];
     const float gam = a.F.gamma_f32 ? a.F.gamma_f32[i] : k.gamma;
+    const float amp_f = k.amp_pref * gam * area;
     float sg = 0.f, lc = 0.f, phr = 0.f, phi = 0.f, l1 = 0.f, l2 = 0.f;
     if (ROUGH != SS_ROUGH_NONE) {
       sg = a.F.sigma ? a.F.sigma[i] : k.sigma;
@@ -145,112 +164,170 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       l1 = sqrtf(dot3f(e1x, e1y, e1z, e1x, e1y, e1z));
       l2 = sqrtf(dot3f(e2x, e2y, e2z, e2x, e2y, e2z));
     }
-    for (int st = 0; st < nt; ++st) {
-      const int tt = rot + st < nt ? rot + st : rot + st - nt;
-      if (i < s_lo[tt] || i >= s_hi[tt]) continue;
-      // --- d = p - c as double-float per component ---
-      float dxh, dxl, dyh, dyl, dzh, dzl, e;
-      two_sum(s_ph[tt][0], -cx, dxh, e);
-      fast_two_sum(dxh, e + s_pl[tt][0], dxh, dxl);
-      two_sum(s_ph[tt][1], -cy, dyh, e);
-      fast_two_sum(dyh, e + s_pl[tt][1], dyh, dyl);
-      two_sum(s_ph[tt][2], -cz, dzh, e);
-      fast_two_sum(dzh, e + s_pl[tt][2], dzh, dzl);
-      // --- S = |d|^2 (double-float) ---
-      float qx, ex, qy, ey, qz, ez;
-      two_prod(dxh, dxh, qx, ex);
-      two_prod(dyh, dyh, qy, ey);
-      two_prod(dzh, dzh, qz, ez);
-      float s1_, e1_, Sh, e2_;
-      two_sum(qx, qy, s1_, e1_);
-      two_sum(s1_, qz, Sh, e2_);
+
+    // --- per-facet reference at the platform of trace `j` ---
+    float qhx, qhy, qhz, qlx, qly, qlz, rch, phc, ubc, fc, cosc, qe1, qe2;
+    float rcl, xnx = 0.f, xny = 0.f, xnz = 0.f;  // q x n (taper's sin^2)
+    auto reference = [&](int j) {
+      float e;
+      two_sum(s_ph[j][0], -cx, qhx, e);
+      fast_two_sum(qhx, e + s_pl[j][0], qhx, qlx);
+      two_sum(s_ph[j][1], -cy, qhy, e);
+      fast_two_sum(qhy, e + s_pl[j][1], qhy, qly);
+      two_sum(s_ph[j][2], -cz, qhz, e);
+      fast_two_sum(qhz, e + s_pl[j][2], qhz, qlz);
+      // S = |q|^2 (double-float), r_c = sqrt(S): rsqrt + one Newton step
+      float sx, ex, sy, ey, sz, ez, s1, e1_, Sh, e2_;
+      two_prod(qhx, qhx, sx, ex);
+      two_prod(qhy, qhy, sy, ey);
+      two_prod(qhz, qhz, sz, ez);
+      two_sum(sx, sy, s1, e1_);
+      two_sum(s1, sz, Sh, e2_);
       float Sl = (e1_ + e2_) + (ex + ey + ez) +
-                 2.0f * (dxh * dxl + dyh * dyl + dzh * dzl);
+                 2.0f * (qhx * qlx + qhy * qly + qhz * qlz);
       fast_two_sum(Sh, Sl, Sh, Sl);
-      // --- r = sqrt(S): rsqrt + one Newton correction ---
       const float y = rsqrtf(Sh);
       const float r0 = Sh * y;
       const float res = __fmaf_rn(-r0, r0, Sh) + Sl;
-      float rh, rl;
-      fast_two_sum(r0, res * (0.5f * y), rh, rl);
-      const float inv_r = y;
-      // --- amplitude (float32) ---
-      const float rx = dxh * inv_r, ry = dyh * inv_r, rz = dzh * inv_r;
-      const float cosv = dot3f(rx, ry, rz, nx, ny, nz);
-      // r_hat . e: the sinc argument k (r_hat . e) reaches tens of radians,
-      // and its products cancel to ~1e-2 of their size near nadir, so the
-      // dot product is formed error-free (two_prod) from the double-float d
-      const float d1 = dot_df(dxh, dxl, dyh, dyl, dzh, dzl, e1x, e1y, e1z) *
-                       inv_r;
-      const float d2 = dot_df(dxh, dxl, dyh, dyl, dzh, dzl, e2x, e2y, e2z) *
-                       inv_r;
-      const float inv_r2 = inv_r * inv_r;
-      float amp = k.amp_pref * gam * cosv * area * sinc32(k.k * d1) *
-                  sinc32(k.k * d2) * inv_r2;
+      fast_two_sum(r0, res * (0.5f * y), rch, rcl);
+      // phase 2 k r_c mod 2 pi (double-float product, exact first step)
+      float ph, pe;
+      two_prod(k.K2h, rch, ph, pe);
+      const float pl = pe + __fmaf_rn(k.K2h, rcl, k.K2l * rch);
+      const float n2 = rintf(ph * 0.159154943091895336f);
+      const float red = __fmaf_rn(-n2, 6.28318548202514648f, ph);
+      phc = __fmaf_rn(-n2, -1.74845553146951e-07f, red) + pl;
+      // bin position u = r_c A - B = ubc + fc
+      float up, ue, us, ue2;
+      two_prod(rch, k.Ah, up, ue);
+      two_sum(up, -k.Bh, us, ue2);
+      const float ul = (ue2 + ue) + __fmaf_rn(rch, k.Al, rcl * k.Ah) - k.Bl;
+      ubc = floorf(us);
+      fc = (us - ubc) + ul;
+      // cos of incidence at the reference, q.n / r_c with q.n from exact
+      // products and a corrected division (~1 ulp): the 0.05 taper turns a
+      // cosine error into a ~400x larger relative amplitude error
+      float pnx, enx, pny, eny, pnz, enz, sn1, es1, qnh, es2;
+      two_prod(qhx, nx, pnx, enx);
+      two_prod(qhy, ny, pny, eny);
+      two_prod(qhz, nz, pnz, enz);
+      two_sum(pnx, pny, sn1, es1);
+      two_sum(sn1, pnz, qnh, es2);
+      const float qnl = (es1 + es2) + (enx + eny + enz) +
+                        dot3f(qlx, qly, qlz, nx, ny, nz);
+      const float yc = __frcp_rn(rch);
+      const float c0 = qnh * yc;
+      const float ce = __fmaf_rn(-c0, rch, qnh) + qnl - c0 * rcl;
+      cosc = __fmaf_rn(ce, yc, c0);
       if (a.taper) {
-        float cc = fminf(fmaxf(cosv, 1e-9f), 1.0f);
-        float c2 = cc * cc;
-        amp *= __expf(-__fdividef(1.0f - c2, c2) * k.taper_inv);
+        xnx = __fmaf_rn(qhy, nz, -qhz * ny) + __fmaf_rn(qly, nz, -qlz * ny);
+        xny = __fmaf_rn(qhz, nx, -qhx * nz) + __fmaf_rn(qlz, nx, -qlx * nz);
+        xnz = __fmaf_rn(qhx, ny, -qhy * nx) + __fmaf_rn(qlx, ny, -qly * nx);
+      }
+      // products with the edge vectors (q_lo matters for the sinc
+      // arguments: k (r_hat . e) reaches tens of radians)
+      qe1 = dot3f(qhx, qhy, qhz, e1x, e1y, e1z) +
+            dot3f(qlx, qly, qlz, e1x, e1y, e1z);
+      qe2 = dot3f(qhx, qhy, qhz, e2x, e2y, e2z) +
+            dot3f(qlx, qly, qlz, e2x, e2y, e2z);
+    };
+
+    // --- one pair: facet i, trace tt at offset w (hi, |w|^2) + wl (lo) ---
+    auto pair = [&](int tt, float4 w, float4 wl) -> float {
+      // N = r_t^2 - r_c^2 = 2 q.w + |w|^2 (q and w as hi + lo)
+      const float corr = __fmaf_rn(
+          qhx, wl.x, __fmaf_rn(qhy, wl.y, __fmaf_rn(
+              qhz, wl.z, __fmaf_rn(qlx, w.x, __fmaf_rn(qly, w.y,
+                                                       qlz * w.z)))));
+      const float qw = __fmaf_rn(qhx, w.x, __fmaf_rn(qhy, w.y,
+                                                     __fmaf_rn(qhz, w.z,
+                                                               corr)));
+      const float N = __fmaf_rn(2.0f, qw, w.w);
+      const float rr = __fmaf_rn(rch, rch, N);
+      const float inv_r = rsqrtf(rr);
+      const float dr = __fdividef(N, rch + rr * inv_r);
+      // --- amplitude (float32) ---
+      // cos_t = (q.n + w.n) / r_t = cos_c + (w.n - cos_c dr) / r_t
+      const float cosv = __fmaf_rn(
+          __fmaf_rn(-cosc, dr, dot3f(nx, ny, nz, w.x, w.y, w.z)), inv_r,
+          cosc);
+      const float d1 = (qe1 + dot3f(e1x, e1y, e1z, w.x, w.y, w.z)) * inv_r;
+      const float d2 = (qe2 + dot3f(e2x, e2y, e2z, w.x, w.y, w.z)) * inv_r;
+      const float inv_r2 = inv_r * inv_r;
+      float amp = amp_f * cosv * sinc32(k.k * d1) * sinc32(k.k * d2) *
+                  inv_r2;
+      if (a.taper) {
+        // tan^2 = sin^2 / cos^2 with sin^2 = |(q + w) x n|^2 / r_t^2 (no
+        // 1 - cos^2 cancellation near nadir)
+        const float sx = xnx + __fmaf_rn(w.y, nz, -w.z * ny);
+        const float sy = xny + __fmaf_rn(w.z, nx, -w.x * nz);
+        const float sz = xnz + __fmaf_rn(w.x, ny, -w.y * nx);
+        const float s2 = dot3f(sx, sy, sz, sx, sy, sz) * inv_r2;
+        const float cc = fminf(fmaxf(cosv, 1e-9f), 1.0f);
+        amp *= __expf(-__fdividef(s2, cc * cc) * k.taper_inv);
       }
       float cr = amp, ci = 0.0f;
       if (ROUGH != SS_ROUGH_NONE) {
         const float kk = 2.0f * k.k * cosv;
-        const float dp = d_phi32<ROUGH>(a.n_terms, lg, s_fad, k.fadL, sg, lc,
-                                        kk, 2.0f * k.k * d1 / l1,
+        const float dp = d_phi32<ROUGH>(a.n_terms, nullptr, s_fad, k.fadL,
+                                        sg, lc, kk, 2.0f * k.k * d1 / l1,
                                         2.0f * k.k * d2 / l2, l1, l2);
-        const float amp_i =
-            area > 0.0f ? k.amp_pref * gam * cosv * inv_r2 * sqrtf(dp) : 0.0f;
+        const float amp_i = area > 0.0f ? k.amp_pref * gam * cosv * inv_r2 *
+                                              sqrtf(dp)
+                                        : 0.0f;
         const float sk = sg * kk;
         const float att = __expf(-0.5f * sk * sk);
         cr = amp * att + amp_i * phr;
         ci = amp_i * phi;
       }
-      // --- carrier phase 2 k r mod 2 pi (double-float) ---
-      float ph, pe;
-      two_prod(k.K2h, rh, ph, pe);
-      const float pl = pe + __fmaf_rn(k.K2h, rl, k.K2l * rh);
-      const float n2 = rintf(ph * 0.159154943091895336f);
-      float red = __fmaf_rn(-n2, 6.28318548202514648f, ph);  // exact
-      red = __fmaf_rn(-n2, -1.74845553146951e-07f, red) + pl;
+      // --- carrier phase: phc + 2 k dr (exact product, exact first step) ---
+      float pp, pe;
+      two_prod(k.K2h, dr, pp, pe);
+      pe = __fmaf_rn(k.K2l, dr, pe);
+      const float n2 = rintf(pp * 0.159154943091895336f);
+      float red = __fmaf_rn(-n2, 6.28318548202514648f, pp);
+      red = __fmaf_rn(-n2, -1.74845553146951e-07f, red) + (pe + phc);
       float sn, cs;
       __sincosf(red, &sn, &cs);
       float re = cr * sn - ci * cs;
       float im = cr * cs + ci * sn;
+      const float qtx = qhx + w.x, qty = qhy + w.y, qtz = qhz + w.z;
       if (a.pat_kind != SS_PAT_ISOTROPIC) {
         const float g = gain32(a.pat_kind, a.pat_n, pa_len, s_pat, s_pv[tt],
-                               -rx, -ry, -rz);
+                               -qtx * inv_r, -qty * inv_r, -qtz * inv_r);
         re *= g * g;
         im *= g * g;
       }
-      // --- bin: u = r A - B (double-float), exact re-bin near edges ---
-      float up, ue, us, ue2;
-      two_prod(rh, k.Ah, up, ue);
-      two_sum(up, -k.Bh, us, ue2);
-      const float ul = (ue2 + ue) + __fmaf_rn(rh, k.Al, rl * k.Ah) - k.Bl;
-      float fb = floorf(us);
-      float frac = (us - fb) + ul;
+      // --- bin: u = ubc + fc + A dr, exact re-bin near edges ---
+      float dh, de;
+      two_prod(k.Ah, dr, dh, de);
+      const float sb = fc + dh;
+      const float fl = floorf(sb);
+      float frac = (sb - fl) + __fmaf_rn(k.Al, dr, de);
+      float fb = ubc + fl;
       if (frac < 0.0f) { fb -= 1.0f; frac += 1.0f; }
       else if (frac >= 1.0f) { fb += 1.0f; frac -= 1.0f; }
-      if ((frac < 1e-6f || frac > 0.999999f) && us > -4.0f &&
-          us < nsf + 4.0f) {
+      if ((frac < guard || frac > 1.0f - guard) && fb > -4.0f &&
+          fb < nsf + 4.0f) {
         // float64 round-to-nearest chain, identical to the oracle
         const double ddx = __dsub_rn(s_p64[tt][0], (double)cx);
         const double ddy = __dsub_rn(s_p64[tt][1], (double)cy);
         const double ddz = __dsub_rn(s_p64[tt][2], (double)cz);
-        const double rr = __dsqrt_rn(__dadd_rn(
+        const double rd = __dsqrt_rn(__dadd_rn(
             __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)),
             __dmul_rn(ddz, ddz)));
         const double u64 = __ddiv_rn(
-            __dsub_rn(__ddiv_rn(__dmul_rn(2.0, rr), a.c), a.t0), a.dt);
+            __dsub_rn(__ddiv_rn(__dmul_rn(2.0, rd), a.c), a.t0), a.dt);
         const double f64b = floor(u64);
         fb = (float)f64b;
         frac = (float)(u64 - f64b);
       }
       int side_off = 0;
       if (a.split &&
-          dot3f(-dxh, -dyh, -dzh, s_u[tt][0], s_u[tt][1], s_u[tt][2]) > 0.0f)
+          dot3f(-qtx, -qty, -qtz, s_u[tt][0], s_u[tt][1], s_u[tt][2]) > 0.0f)
         side_off = a.n_samples;
       float2 *h = hist + (size_t)tt * a.n_seg + side_off;
+      float drop = 0.0f;
       if (a.interp) {
         const float wq[2] = {1.0f - frac, frac};
 #pragma unroll
@@ -261,19 +338,47 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
             atomicAdd(&h[(int)bq].x, pr);
             atomicAdd(&h[(int)bq].y, pim);
           } else {
-            dropl[tt] += pr * pr + pim * pim;
+            drop += pr * pr + pim * pim;
           }
         }
       } else if (fb >= 0.0f && fb < nsf) {
         atomicAdd(&h[(int)fb].x, re);
         atomicAdd(&h[(int)fb].y, im);
       } else {
-        dropl[tt] += re * re + im * im;
+        drop = re * re + im * im;
+      }
+      return drop;
+    };
+
+    if (ref >= 0) {
+      reference(ref);
+#pragma unroll 1
+      for (int st = 0; st < nt; ++st) {
+        const int tt = rot + st < nt ? rot + st : rot + st - nt;
+        const int2 win = s_win[tt];
+        if (i >= win.x && i < win.y) {
+          const float d = pair(tt, s_w[tt], s_wl[tt]);
+          if (d != 0.0f) dropl[st] += d;
+        }
+      }
+    } else {
+      for (int tt = 0; tt < nt; ++tt) {
+        const int2 win = s_win[tt];
+        if (i < win.x || i >= win.y) continue;
+        reference(tt);
+        const float d = pair(tt, make_float4(0.f, 0.f, 0.f, 0.f),
+                             make_float4(0.f, 0.f, 0.f, 0.f));
+        if (d != 0.0f) atomicAdd(&s_drop[tt], d);
       }
     }
   }
-  for (int tt = 0; tt < nt; ++tt)
-    if (dropl[tt] != 0.0f) atomicAdd(&s_drop[tt], dropl[tt]);
+#pragma unroll
+  for (int st = 0; st < SS_MAX_TB; ++st) {
+    if (st < nt && dropl[st] != 0.0f) {
+      const int tt = rot + st < nt ? rot + st : rot + st - nt;
+      atomicAdd(&s_drop[tt], dropl[st]);
+    }
+  }
   __syncthreads();
   float2 *part = reinterpret_cast<float2 *>(a.part);
   for (int tt = 0; tt < nt; ++tt) {
@@ -285,8 +390,12 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
     a.part_drop[(size_t)chunk * a.T + t_base + tid] = (double)s_drop[tid];
 }
 
+// Four 256-thread CTAs per SM (64 registers) for smooth facets, three (80
+// registers, no spills) when the roughness series is inlined.
+#define SS_SPLIT_CTAS(R) ((R) == SS_ROUGH_NONE ? 4 : 3)
+
 template <int ROUGH>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, SS_SPLIT_CTAS(ROUGH))
 coherent_split_kernel(CoArgs a, SplitConsts k) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   coherent_split_cta<ROUGH>(a, k, blockIdx.x, blockIdx.y, smem_raw);
@@ -296,7 +405,7 @@ coherent_split_kernel(CoArgs a, SplitConsts k) {
 // items from a global counter until the queue is empty, so jobs of very
 // different sizes share one launch without tail effects.
 template <int ROUGH>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, SS_SPLIT_CTAS(ROUGH))
 coherent_batch_split_kernel(const BatchJob *jobs, int n_jobs,
                             long long n_items, unsigned long long *counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -412,8 +521,7 @@ int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st) {
   }
   const SplitConsts k = coherent_split_consts(a);
   dim3 grid(p.n_chunks, p.n_groups);
-  size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2) +
-                (a.rough_kind ? (a.n_terms + 1) * sizeof(float) : 0);
+  size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2);
   cudaError_t e = cudaSuccess;
   switch (a.rough_kind) {
 #define SS_LAUNCH(R)                                                         \

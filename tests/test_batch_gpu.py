@@ -64,7 +64,21 @@ def test_batch_matches_oracle_and_one_call(jobs, precision):
         np.testing.assert_allclose(drop, d1, rtol=1e-5, atol=1e-9 * scale ** 2)
 
 
+def _close(f, r, tol):
+    """Max error within ``tol`` of the peak and relative L2 within tol/10."""
+    peak = r.abs().max().item()
+    rel = (torch.linalg.vector_norm(f - r) /
+           torch.linalg.vector_norm(r)).item()
+    return torch.allclose(f, r, rtol=0, atol=tol * peak) and rel <= tol / 10
+
+
 def test_graph_replay_and_tunings_agree(jobs):
+    """The graph replay equals the eager run to float32 summation order
+    (2e-6 of the peak). Other tunings change each trace block's reference
+    trace (the middle of 2, 4 or 8 traces; blocks wider than 64 m take a
+    reference per trace), and with it the float32 range difference of every
+    pair (relative error < 6e-7 of |p_t - p_c| <= 160 m here): they agree
+    to 2e-5 of the peak and 2e-6 relative L2."""
     b, res = _run(jobs, "split", tuning=(128, 2, 64, 0))
     ref = [f.clone() for f, _ in b.outputs]
     for f, d in b.outputs:
@@ -83,7 +97,7 @@ def test_graph_replay_and_tunings_agree(jobs):
     b.run()
     torch.cuda.synchronize()
     for (f, _), r in zip(b.outputs, ref):
-        assert torch.allclose(f, r, rtol=0, atol=2e-6 * r.abs().max().item())
+        assert _close(f, r, 2e-5)
 
 
 def test_batch_rejects_mixed_roughness(jobs, golden):
