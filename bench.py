@@ -956,8 +956,9 @@ def row_cfg4(device, n_inst, flush, peaks, cpu_seconds=0.0):
     host_s = time.perf_counter() - t_host
     batch = CoherentBatch(plans)
     tun, tune_ms = batch.autotune(
-        candidates=[(256, 8, 16, 0), (256, 4, 16, 0), (128, 8, 16, 0),
-                    (256, 8, 4, 0), (256, 8, 64, 0), (128, 4, 64, 0)],
+        candidates=[(512, 8, 16, 0), (512, 6, 16, 0), (256, 8, 16, 0),
+                    (256, 4, 16, 0), (128, 8, 16, 0), (512, 6, 64, 0),
+                    (256, 8, 64, 0), (128, 4, 64, 0)],
         reps=1)
     batch.capture()
     ms = _events_ms(batch.replay, 3, flush)

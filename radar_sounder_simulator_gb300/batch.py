@@ -41,8 +41,10 @@ BatchInfo = _lib.BatchInfo
 
 
 DEFAULT_TUNING = (256, 8, 16, 0)
+# (512-thread CTAs take smooth split-precision batches only; a batch that
+# refuses a candidate skips it)
 CANDIDATES = [(t, tb, ips, 0) for t, tb, ips in itertools.product(
-    (128, 256), (2, 4, 8), (4, 16, 64))]
+    (128, 256, 512), (2, 4, 8), (4, 16, 64))]
 
 
 class CoherentBatch:

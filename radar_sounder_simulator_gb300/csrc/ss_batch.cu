@@ -39,8 +39,8 @@ static int batch_layout(const ss_coherent_job *jobs, int n_jobs,
     return SS_ERR_ARG;
   }
   const int threads = tune && tune->threads ? tune->threads : 256;
-  if (threads != 128 && threads != 256) {
-    set_error("batch threads must be 128 or 256");
+  if (threads != 128 && threads != 256 && threads != 512) {
+    set_error("batch threads must be 128, 256 or 512");
     return SS_ERR_ARG;
   }
   const int max_tb = tune && tune->max_tb ? tune->max_tb : SS_MAX_TB;
@@ -70,6 +70,11 @@ static int batch_layout(const ss_coherent_job *jobs, int n_jobs,
     } else if (a.precision != L.precision || a.rough_kind != L.rough_kind) {
       set_error("all jobs of a batch need the same precision and roughness "
                 "kind");
+      return SS_ERR_ARG;
+    }
+    if (threads == 512 &&
+        (a.precision == SS_PREC_FP64 || a.rough_kind != SS_ROUGH_NONE)) {
+      set_error("512-thread batches take smooth split-precision jobs only");
       return SS_ERR_ARG;
     }
     const size_t elt = a.precision == SS_PREC_FP64 ? 16 : 8;
@@ -112,7 +117,10 @@ static int batch_layout(const ss_coherent_job *jobs, int n_jobs,
     const size_t lg = a.rough_kind && a.precision == SS_PREC_FP64
                           ? (size_t)(a.n_terms + 1) * 8
                           : 0;
-    L.smem = std::max(L.smem, (size_t)a.tb * a.n_seg * elt + lg);
+    const size_t hist = a.precision == SS_PREC_FP64
+                            ? (size_t)a.tb * a.n_seg * elt
+                            : split_hist_bytes(a.n_seg, a.tb);
+    L.smem = std::max(L.smem, hist + lg);
   }
   L.n_items = item;
   L.n_out = out;

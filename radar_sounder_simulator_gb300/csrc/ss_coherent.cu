@@ -239,17 +239,20 @@ int batch_fp64_blocks_per_sm(int threads, size_t smem) {
 // ---------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------
-int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p) {
+int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p,
+                  bool rough) {
   if (o->n_samples <= 0 || T <= 0 || N <= 0 || o->block_size <= 0 ||
       o->n_win <= 0)
     return SS_ERR_ARG;
   const int n_seg = o->n_samples * (o->split_sides ? 2 : 1);
-  const size_t elt = o->precision == SS_PREC_FP64 ? 16 : 8;
-  // split form: 48 KB of histograms per 256-thread CTA lets four CTAs (32
-  // warps, the register limit at 64 registers) share an SM, which hides the
-  // shared-memory atomic latency of this short per-pair computation (a
-  // 100 KB budget allowed two: 7.6 -> 5.7 ms on the 512^2 x 1024 surface)
-  const size_t budget = o->precision == SS_PREC_FP64 ? 96 * 1024 : 48 * 1024;
+  const bool fp64 = o->precision == SS_PREC_FP64;
+  const size_t elt = fp64 ? 16 : 8;
+  // split form: 32 resident warps per SM at 64 registers hide the
+  // shared-memory atomic latency of this short per-pair computation. Smooth
+  // facets run two 512-thread CTAs of 96 KB of histograms (six traces of
+  // 2048 bins share each facet's double-float reference); the roughness
+  // series needs 80 registers, so three 256-thread CTAs of 48 KB.
+  const size_t budget = fp64 ? 96 * 1024 : (rough ? 48 * 1024 : 96 * 1024);
   const size_t per_trace = (size_t)n_seg * elt;
   if (per_trace > 200 * 1024) return SS_ERR_UNSUPPORTED;
   int tb = (int)std::max<size_t>(1, std::min<size_t>(budget / per_trace,
@@ -257,7 +260,7 @@ int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p) {
   tb = std::min(tb, T);
   p->tb = tb;
   p->n_groups = (T + tb - 1) / tb;
-  p->threads = 256;
+  p->threads = fp64 || rough ? 256 : 512;
   const long window = std::min<long>((long)o->n_win * o->block_size, N);
   const int max_chunks = (int)std::max<long>(1, window / 512);
   const int target = 4 * sm_count();
@@ -268,8 +271,13 @@ int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p) {
 }
 
 size_t coherent_scratch(const ss_coherent_opts *o, int T, int N) {
-  Plan p;
-  if (coherent_plan(o, T, N, &p) != SS_OK) return 0;
+  // the options do not say whether the facets are rough: size for the
+  // larger chunk count of the two plans
+  Plan p, pr;
+  if (coherent_plan(o, T, N, &p, false) != SS_OK ||
+      coherent_plan(o, T, N, &pr, true) != SS_OK)
+    return 0;
+  p.n_chunks = std::max(p.n_chunks, pr.n_chunks);
   const int n_seg = o->n_samples * (o->split_sides ? 2 : 1);
   const size_t elt = o->precision == SS_PREC_FP64 ? 16 : 8;
   size_t hist = (size_t)p.n_chunks * T * n_seg * elt;
@@ -338,7 +346,8 @@ int build_co_args(const ss_coherent_opts *opts, const ss_facets *facets,
     set_error("unknown precision");
     return SS_ERR_ARG;
   }
-  int s = coherent_plan(opts, T, N, &p);
+  int s = coherent_plan(opts, T, N, &p,
+                        rough && rough->kind != SS_ROUGH_NONE);
   if (s) {
     set_error(s == SS_ERR_UNSUPPORTED ? "n_samples too large for the "
                                         "shared-memory histogram"

@@ -22,13 +22,26 @@ struct CoArgs {
   double *part_drop;   // (n_chunks, T) partial dropped power
 };
 
-int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p);
+int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p,
+                  bool rough);
 size_t coherent_scratch(const ss_coherent_opts *o, int T, int N);
 int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st);
 int build_co_args(const ss_coherent_opts *opts, const ss_facets *facets,
                   const ss_traces *traces, const ss_pattern *pattern,
                   const ss_roughness *rough, const ss_output *out, Plan &p,
                   CoArgs &a);
+
+// Shared-memory histograms of the split coherent kernel: planar real and
+// imaginary planes of `tb` traces each, a trace's row padded to n_seg + 11
+// floats so the block's traces start 11 banks apart (neighbouring facets
+// of a warp, spread over the traces, then rarely meet in one bank).
+__host__ __device__ __forceinline__ int split_hist_stride(int n_seg) {
+  return n_seg + 11;
+}
+__host__ __device__ __forceinline__ size_t split_hist_bytes(int n_seg,
+                                                            int tb) {
+  return (size_t)2 * tb * split_hist_stride(n_seg) * sizeof(float);
+}
 
 // float32 / double-float constants of the split coherent kernel.
 struct SplitConsts {

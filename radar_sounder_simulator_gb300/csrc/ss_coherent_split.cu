@@ -13,20 +13,23 @@
 //     exact), its bin position split into an integer and a fraction, and the
 //     products of q = p_c - c with the facet's normal and edge vectors.
 //   * Per trace t of the block, with w = p_t - p_c (a few trace spacings):
-//     r_t^2 - r_c^2 = 2 q.w + |w|^2 = N, so r_t - r_c = N / (r_c + r_t) in
-//     float32. Its relative error is below 6e-7 (three roundings of the
-//     2 q.w sum against D = 2r, the rsqrt of r_t and the division), so the
-//     absolute error is below 6e-7 |w|: 1.5e-5 m for a 25 m spacing, 2.8e-4
-//     rad of phase at 450 MHz in the worst case and ~5e-5 rad typically.
-//     The middle trace has w = 0 and its pairs are exact to the reference's
+//     r_t^2 - r_c^2 = 2 q.w + |w|^2 = N, so r_t - r_c = N / (r_c + r_t).
+//     N is a double-float (exact products, compensated sums), the division
+//     takes a float32 quotient and one correction against the double-float
+//     denominator 2 r_c + dr, so dr = r_t - r_c is good to ~2e-11 of its
+//     size (3e-9 m at |w| = 160 m; a float32 dr would carry ulp(|w|)/2 of
+//     rounding: 4e-6 m at 100 m, 8e-5 rad of phase at 450 MHz). The middle
+//     trace has w = 0 and its pairs are exact to the reference's
 //     double-float.
 //
-// The bin of a pair within 4e-6 + 1e-6 |w|_max A bins of an edge (A = 2 /
-// (c dt), bins per metre) is decided by the float64 round-to-nearest chain
-// of the oracle, so bins are bit-identical to the float64 form: the band
-// is twice the largest error of the float32 bin position. A block whose
-// traces lie more than 64 m from its middle trace (sparse or crooked
-// tracks) takes a reference per trace instead (w = 0 for every pair).
+// The bin position ubc + fc + A dr is then good to ~2e-7 bins; a pair
+// within 2e-6 bins of an edge recomputes its own double-float range and
+// bin (~1e-10 bins, FP32 pipe), and only within 1e-8 bins of an edge does
+// the float64 round-to-nearest chain of the oracle decide, so bins are
+// bit-identical to the float64 form while the slow FP64 pipe almost never
+// runs. A block whose traces lie more than 160 m from its middle trace
+// (sparse or crooked tracks) takes a reference per trace instead (w = 0
+// for every pair).
 //
 // Everything else (incidence, sincs, taper, antenna gain, roughness series)
 // runs in float32 from q + w and the facet's per-block products;
@@ -40,8 +43,18 @@
 
 namespace ss {
 
-// Widest trace block (largest |p_t - p_c|, metres) served by one reference.
-constexpr float kWideBlock = 64.0f;
+// Widest trace block (largest |p_t - p_c|, metres) served by one reference:
+// eight traces at 40 m.
+constexpr float kWideBlock = 160.0f;
+// Bin-edge band of the per-trace bin position (~10x its error).
+constexpr float kBinBand = 2e-6f;
+
+// Integer value of an integral float with |x| < 2^22: adding 1.5 * 2^23
+// places it in the low mantissa bits (exact), read back as an integer --
+// two FP32/integer-pipe instructions instead of a conversion.
+__device__ __forceinline__ int small_int(float x) {
+  return __float_as_int(x + 12582912.0f) - 0x4B400000;
+}
 
 // One CTA's work item: facet chunk `chunk` of trace block `group`. Shared
 // by the one-call kernel (item = block index) and the batched persistent
@@ -51,11 +64,14 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
                                                    const SplitConsts &k,
                                                    int chunk, int group,
                                                    unsigned char *smem_raw) {
-  float2 *hist = reinterpret_cast<float2 *>(smem_raw);
+  const int hs = split_hist_stride(a.n_seg);
+  float *hre = reinterpret_cast<float *>(smem_raw);
+  float *him = hre + (size_t)a.tb * hs;
   __shared__ float s_ph[SS_MAX_TB][3], s_pl[SS_MAX_TB][3];
   __shared__ double s_p64[SS_MAX_TB][3];
   __shared__ float4 s_w[SS_MAX_TB];   // p_t - p_c (hi), |p_t - p_c|^2
-  __shared__ float4 s_wl[SS_MAX_TB];  // p_t - p_c (lo), |p_t - p_c|
+  __shared__ float4 s_wl[SS_MAX_TB];  // p_t - p_c (lo), |p_t - p_c|^2 (lo)
+  __shared__ float s_wn[SS_MAX_TB];    // |p_t - p_c|
   __shared__ float s_u[SS_MAX_TB][3];
   __shared__ float s_pv[SS_MAX_TB][6];
   __shared__ int2 s_win[SS_MAX_TB];
@@ -65,7 +81,6 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   __shared__ int s_rng[2];
   __shared__ int s_next;
   __shared__ int s_ref;      // the block's reference trace; -1: per trace
-  __shared__ float s_guard;  // bin-edge band of the differential form
 
   const int t_base = group * a.tb;
   const int nt = min(a.tb, a.T - t_base);
@@ -88,9 +103,11 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       w2 += w[j] * w[j];
     }
     const float wx = (float)w[0], wy = (float)w[1], wz = (float)w[2];
-    s_w[tid] = make_float4(wx, wy, wz, (float)w2);
+    const float w2h = (float)w2;
+    s_w[tid] = make_float4(wx, wy, wz, w2h);
     s_wl[tid] = make_float4((float)(w[0] - wx), (float)(w[1] - wy),
-                            (float)(w[2] - wz), (float)sqrt(w2));
+                            (float)(w[2] - wz), (float)(w2 - (double)w2h));
+    s_wn[tid] = (float)sqrt(w2);
     for (int j = 0; j < 6; ++j)
       s_pv[tid][j] =
           (a.pv && j < a.pv_len) ? (float)a.pv[a.pv_len * t + j] : 0.0f;
@@ -104,30 +121,26 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
     s_pat[pa_len + j] = (float)a.pb[j];
   if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
     s_fad[tid] = (float)a.fad.a[tid];
-  for (int j = tid; j < a.tb * a.n_seg; j += blockDim.x)
-    hist[j] = make_float2(0.0f, 0.0f);
+  for (int j = tid; j < 2 * a.tb * hs; j += blockDim.x) hre[j] = 0.0f;
   __syncthreads();
   if (tid == 0) {
     int lo = s_win[0].x, hi = s_win[0].y;
-    float wmax = s_wl[0].w;
+    float wmax = s_wn[0];
     for (int j = 1; j < nt; ++j) {
       lo = min(lo, s_win[j].x);
       hi = max(hi, s_win[j].y);
-      wmax = fmaxf(wmax, s_wl[j].w);
+      wmax = fmaxf(wmax, s_wn[j]);
     }
     long len = max(hi - lo, 0);
     s_rng[0] = lo + (int)(len * chunk / a.n_chunks);
     s_rng[1] = lo + (int)(len * (chunk + 1) / a.n_chunks);
     s_next = s_rng[0];
-    const bool one_ref = wmax <= kWideBlock;
-    s_ref = one_ref ? nt / 2 : -1;
-    s_guard = one_ref ? 4e-6f + 1e-6f * wmax * k.Ah : 1e-6f;
+    s_ref = wmax <= kWideBlock ? nt / 2 : -1;
   }
   __syncthreads();
 
   const float nsf = (float)a.n_samples;
   const int ref = s_ref;
-  const float guard = s_guard;
   // lane l meets the block's traces starting at trace l mod nt, so the 32
   // neighbouring facets of a warp -- often in one bin -- spread their
   // histogram atomics over the block's traces; dropped power collects per
@@ -232,20 +245,92 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
             dot3f(qlx, qly, qlz, e2x, e2y, e2z);
     };
 
+    // --- bin of a pair near an edge, decided as the float64 form does ---
+    // First the pair's own double-float range (exact difference of the
+    // double-float platform and the float32 centroid, exact squares, rsqrt +
+    // Newton) and bin position u = r A - B, accurate to ~1e-10 bins on the
+    // FP32 pipe; the float64 round-to-nearest chain of the oracle (~1e-12
+    // bins from the exact u) runs only within 1e-8 bins of an edge, where
+    // the two could round differently.
+    auto exact_bin = [&](int tt, float &fb, float &frac) {
+      float dxh, dxl, dyh, dyl, dzh, dzl, e;
+      two_sum(s_ph[tt][0], -cx, dxh, e);
+      fast_two_sum(dxh, e + s_pl[tt][0], dxh, dxl);
+      two_sum(s_ph[tt][1], -cy, dyh, e);
+      fast_two_sum(dyh, e + s_pl[tt][1], dyh, dyl);
+      two_sum(s_ph[tt][2], -cz, dzh, e);
+      fast_two_sum(dzh, e + s_pl[tt][2], dzh, dzl);
+      float sx, ex, sy, ey, sz, ez, s1, e1_, Sh, e2_;
+      two_prod(dxh, dxh, sx, ex);
+      two_prod(dyh, dyh, sy, ey);
+      two_prod(dzh, dzh, sz, ez);
+      two_sum(sx, sy, s1, e1_);
+      two_sum(s1, sz, Sh, e2_);
+      float Sl = (e1_ + e2_) + (ex + ey + ez) +
+                 2.0f * (dxh * dxl + dyh * dyl + dzh * dzl);
+      fast_two_sum(Sh, Sl, Sh, Sl);
+      const float y = rsqrtf(Sh);
+      const float r0 = Sh * y;
+      const float res = __fmaf_rn(-r0, r0, Sh) + Sl;
+      float rh, rl;
+      fast_two_sum(r0, res * (0.5f * y), rh, rl);
+      float up, ue, us, ue2;
+      two_prod(rh, k.Ah, up, ue);
+      two_sum(up, -k.Bh, us, ue2);
+      const float ul = (ue2 + ue) + __fmaf_rn(rh, k.Al, rl * k.Ah) - k.Bl;
+      float f2 = floorf(us);
+      float fr2 = (us - f2) + ul;
+      if (fr2 < 0.0f) { f2 -= 1.0f; fr2 += 1.0f; }
+      else if (fr2 >= 1.0f) { f2 += 1.0f; fr2 -= 1.0f; }
+      if (fr2 < 1e-8f || fr2 > 1.0f - 1e-8f) {
+        const double ddx = __dsub_rn(s_p64[tt][0], (double)cx);
+        const double ddy = __dsub_rn(s_p64[tt][1], (double)cy);
+        const double ddz = __dsub_rn(s_p64[tt][2], (double)cz);
+        const double rd = __dsqrt_rn(__dadd_rn(
+            __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)),
+            __dmul_rn(ddz, ddz)));
+        const double u64 = __ddiv_rn(
+            __dsub_rn(__ddiv_rn(__dmul_rn(2.0, rd), a.c), a.t0), a.dt);
+        const double f64b = floor(u64);
+        f2 = (float)f64b;
+        fr2 = (float)(u64 - f64b);
+      }
+      fb = f2;
+      frac = fr2;
+    };
+
     // --- one pair: facet i, trace tt at offset w (hi, |w|^2) + wl (lo) ---
     auto pair = [&](int tt, float4 w, float4 wl) -> float {
-      // N = r_t^2 - r_c^2 = 2 q.w + |w|^2 (q and w as hi + lo)
+      // N = r_t^2 - r_c^2 = 2 q.w + |w|^2 as a double-float: exact
+      // products of the hi parts, compensated sums, the lo parts' products
+      // (q_lo.w_hi + q_hi.w_lo) and |w|^2's lo part in float
+      float p1, e1, p2, e2, p3, e3, s1, f1, s2, f2;
+      two_prod(qhx, w.x, p1, e1);
+      two_prod(qhy, w.y, p2, e2);
+      two_prod(qhz, w.z, p3, e3);
+      two_sum(p1, p2, s1, f1);
+      two_sum(s1, p3, s2, f2);
       const float corr = __fmaf_rn(
           qhx, wl.x, __fmaf_rn(qhy, wl.y, __fmaf_rn(
               qhz, wl.z, __fmaf_rn(qlx, w.x, __fmaf_rn(qly, w.y,
                                                        qlz * w.z)))));
-      const float qw = __fmaf_rn(qhx, w.x, __fmaf_rn(qhy, w.y,
-                                                     __fmaf_rn(qhz, w.z,
-                                                               corr)));
-      const float N = __fmaf_rn(2.0f, qw, w.w);
-      const float rr = __fmaf_rn(rch, rch, N);
+      const float lo = (f1 + f2) + (e1 + e2 + e3) + corr;
+      float Nh, g;
+      two_sum(2.0f * s2, w.w, Nh, g);
+      const float Nl = g + __fmaf_rn(2.0f, lo, wl.w);
+      // float32 r_t for the amplitude and a first dr, then dr = N / D with
+      // D = r_c + r_t = 2 r_c + dr as a double-float and one correction:
+      // dr is then good to ~2e-11 of its size
+      const float rr = __fmaf_rn(rch, rch, Nh);
       const float inv_r = rsqrtf(rr);
-      const float dr = __fdividef(N, rch + rr * inv_r);
+      const float dr0 = __fdividef(Nh, rch + rr * inv_r);
+      float Dh, De;
+      fast_two_sum(2.0f * rch, dr0, Dh, De);
+      const float Dl = __fmaf_rn(2.0f, rcl, De);
+      const float iD = __fdividef(1.0f, Dh);
+      const float dr = Nh * iD;
+      const float drl =
+          (__fmaf_rn(-dr, Dh, Nh) + __fmaf_rn(-dr, Dl, Nl)) * iD;
       // --- amplitude (float32) ---
       // cos_t = (q.n + w.n) / r_t = cos_c + (w.n - cos_c dr) / r_t
       const float cosv = __fmaf_rn(
@@ -283,7 +368,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       // --- carrier phase: phc + 2 k dr (exact product, exact first step) ---
       float pp, pe;
       two_prod(k.K2h, dr, pp, pe);
-      pe = __fmaf_rn(k.K2l, dr, pe);
+      pe += __fmaf_rn(k.K2h, drl, k.K2l * dr);
       const float n2 = rintf(pp * 0.159154943091895336f);
       float red = __fmaf_rn(-n2, 6.28318548202514648f, pp);
       red = __fmaf_rn(-n2, -1.74845553146951e-07f, red) + (pe + phc);
@@ -299,34 +384,22 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
         im *= g * g;
       }
       // --- bin: u = ubc + fc + A dr, exact re-bin near edges ---
-      float dh, de;
+      float dh, de, sb, se;
       two_prod(k.Ah, dr, dh, de);
-      const float sb = fc + dh;
+      two_sum(fc, dh, sb, se);
       const float fl = floorf(sb);
-      float frac = (sb - fl) + __fmaf_rn(k.Al, dr, de);
+      float frac = (sb - fl) + (se + de + __fmaf_rn(k.Ah, drl, k.Al * dr));
       float fb = ubc + fl;
       if (frac < 0.0f) { fb -= 1.0f; frac += 1.0f; }
       else if (frac >= 1.0f) { fb += 1.0f; frac -= 1.0f; }
-      if ((frac < guard || frac > 1.0f - guard) && fb > -4.0f &&
-          fb < nsf + 4.0f) {
-        // float64 round-to-nearest chain, identical to the oracle
-        const double ddx = __dsub_rn(s_p64[tt][0], (double)cx);
-        const double ddy = __dsub_rn(s_p64[tt][1], (double)cy);
-        const double ddz = __dsub_rn(s_p64[tt][2], (double)cz);
-        const double rd = __dsqrt_rn(__dadd_rn(
-            __dadd_rn(__dmul_rn(ddx, ddx), __dmul_rn(ddy, ddy)),
-            __dmul_rn(ddz, ddz)));
-        const double u64 = __ddiv_rn(
-            __dsub_rn(__ddiv_rn(__dmul_rn(2.0, rd), a.c), a.t0), a.dt);
-        const double f64b = floor(u64);
-        fb = (float)f64b;
-        frac = (float)(u64 - f64b);
-      }
+      if ((frac < kBinBand || frac > 1.0f - kBinBand) && fb > -4.0f &&
+          fb < nsf + 4.0f)
+        exact_bin(tt, fb, frac);
       int side_off = 0;
       if (a.split &&
           dot3f(-qtx, -qty, -qtz, s_u[tt][0], s_u[tt][1], s_u[tt][2]) > 0.0f)
         side_off = a.n_samples;
-      float2 *h = hist + (size_t)tt * a.n_seg + side_off;
+      const int row = tt * hs + side_off;
       float drop = 0.0f;
       if (a.interp) {
         const float wq[2] = {1.0f - frac, frac};
@@ -335,15 +408,17 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
           const float bq = fb + (float)q;
           const float pr = re * wq[q], pim = im * wq[q];
           if (bq >= 0.0f && bq < nsf) {
-            atomicAdd(&h[(int)bq].x, pr);
-            atomicAdd(&h[(int)bq].y, pim);
+            const int j = row + small_int(bq);
+            atomicAdd(hre + j, pr);
+            atomicAdd(him + j, pim);
           } else {
             drop += pr * pr + pim * pim;
           }
         }
       } else if (fb >= 0.0f && fb < nsf) {
-        atomicAdd(&h[(int)fb].x, re);
-        atomicAdd(&h[(int)fb].y, im);
+        const int j = row + small_int(fb);
+        atomicAdd(hre + j, re);
+        atomicAdd(him + j, im);
       } else {
         drop = re * re + im * im;
       }
@@ -384,18 +459,20 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   for (int tt = 0; tt < nt; ++tt) {
     const size_t base = ((size_t)chunk * a.T + t_base + tt) * a.n_seg;
     for (int j = tid; j < a.n_seg; j += blockDim.x)
-      part[base + j] = hist[(size_t)tt * a.n_seg + j];
+      part[base + j] = make_float2(hre[tt * hs + j], him[tt * hs + j]);
   }
   if (tid < nt)
     a.part_drop[(size_t)chunk * a.T + t_base + tid] = (double)s_drop[tid];
 }
 
-// Four 256-thread CTAs per SM (64 registers) for smooth facets, three (80
-// registers, no spills) when the roughness series is inlined.
-#define SS_SPLIT_CTAS(R) ((R) == SS_ROUGH_NONE ? 4 : 3)
+// Smooth facets: up to 512 threads, 64 registers (two 512-thread or four
+// 256-thread CTAs per SM). With the roughness series inlined: up to 256
+// threads, 80 registers (three CTAs per SM, no spills).
+#define SS_SPLIT_MAXT(R) ((R) == SS_ROUGH_NONE ? 512 : 256)
+#define SS_SPLIT_MINB(R) ((R) == SS_ROUGH_NONE ? 2 : 3)
 
 template <int ROUGH>
-__global__ void __launch_bounds__(256, SS_SPLIT_CTAS(ROUGH))
+__global__ void __launch_bounds__(SS_SPLIT_MAXT(ROUGH), SS_SPLIT_MINB(ROUGH))
 coherent_split_kernel(CoArgs a, SplitConsts k) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   coherent_split_cta<ROUGH>(a, k, blockIdx.x, blockIdx.y, smem_raw);
@@ -405,7 +482,7 @@ coherent_split_kernel(CoArgs a, SplitConsts k) {
 // items from a global counter until the queue is empty, so jobs of very
 // different sizes share one launch without tail effects.
 template <int ROUGH>
-__global__ void __launch_bounds__(256, SS_SPLIT_CTAS(ROUGH))
+__global__ void __launch_bounds__(SS_SPLIT_MAXT(ROUGH), SS_SPLIT_MINB(ROUGH))
 coherent_batch_split_kernel(const BatchJob *jobs, int n_jobs,
                             long long n_items, unsigned long long *counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -521,7 +598,7 @@ int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st) {
   }
   const SplitConsts k = coherent_split_consts(a);
   dim3 grid(p.n_chunks, p.n_groups);
-  size_t smem = (size_t)p.tb * a.n_seg * sizeof(float2);
+  size_t smem = split_hist_bytes(a.n_seg, p.tb);
   cudaError_t e = cudaSuccess;
   switch (a.rough_kind) {
 #define SS_LAUNCH(R)                                                         \

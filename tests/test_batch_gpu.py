@@ -75,10 +75,10 @@ def _close(f, r, tol):
 def test_graph_replay_and_tunings_agree(jobs):
     """The graph replay equals the eager run to float32 summation order
     (2e-6 of the peak). Other tunings change each trace block's reference
-    trace (the middle of 2, 4 or 8 traces; blocks wider than 64 m take a
-    reference per trace), and with it the float32 range difference of every
-    pair (relative error < 6e-7 of |p_t - p_c| <= 160 m here): they agree
-    to 2e-5 of the peak and 2e-6 relative L2."""
+    trace (the middle of 2, 4 or 8 traces at 40 m), and with it the float32
+    range difference of every pair (error < 6e-7 of |p_t - p_c| <= 160 m
+    by the rounding bound, ~2e-8 of it in practice): they agree to 2e-5 of
+    the peak and 2e-6 relative L2."""
     b, res = _run(jobs, "split", tuning=(128, 2, 64, 0))
     ref = [f.clone() for f, _ in b.outputs]
     for f, d in b.outputs:
