@@ -263,9 +263,24 @@ int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p,
   p->threads = fp64 || rough ? 256 : 512;
   const long window = std::min<long>((long)o->n_win * o->block_size, N);
   const int max_chunks = (int)std::max<long>(1, window / 512);
-  const int target = 4 * sm_count();
-  p->n_chunks = std::max(1, std::min(max_chunks,
-                                     (target + p->n_groups - 1) / p->n_groups));
+  // resident CTAs per SM: 2 (512-thread smooth split, 96 KB FP64), 3
+  // (rough split at 80 registers); the chunk count whose item total fills
+  // 2-4 whole waves best (a last wave a tenth full costs a full wave)
+  const long slots = (long)sm_count() * (fp64 ? 2 : (rough ? 3 : 2));
+  int best = 1;
+  double best_eff = -1.0;
+  for (int k = 2; k <= 4; ++k) {
+    const int nc = (int)std::max<long>(
+        1, std::min<long>(max_chunks, k * slots / p->n_groups));
+    const long items = (long)nc * p->n_groups;
+    const long waves = (items + slots - 1) / slots;
+    const double eff = (double)items / (double)(waves * slots);
+    if (eff > best_eff + 1e-9) {
+      best_eff = eff;
+      best = nc;
+    }
+  }
+  p->n_chunks = best;
   p->smem = (size_t)tb * per_trace + (SS_MAX_TERMS + 1) * sizeof(double);
   return SS_OK;
 }

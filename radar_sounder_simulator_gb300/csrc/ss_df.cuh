@@ -103,6 +103,51 @@ __device__ __forceinline__ df df_norm3(df x, df y, df z) {
   return df_make(r0, res * (0.5f * r));
 }
 
+__device__ __forceinline__ df df_neg(df a) { return df{-a.hi, -a.lo}; }
+
+__device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+
+__device__ __forceinline__ df df_abs(df a) {
+  return a.hi < 0.0f || (a.hi == 0.0f && a.lo < 0.0f) ? df_neg(a) : a;
+}
+
+// a < b for renormalised double-floats.
+__device__ __forceinline__ bool df_lt(df a, df b) {
+  return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+
+__device__ __forceinline__ df df_max(df a, df b) { return df_lt(a, b) ? b : a; }
+__device__ __forceinline__ df df_min(df a, df b) { return df_lt(a, b) ? a : b; }
+
+// a / b: a float32 quotient and two corrections against the double-float
+// remainder (~2^-46 relative).
+__device__ __forceinline__ df df_div(df a, df b) {
+  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const df r1 = df_sub(a, df_mul_f(b, q1));
+  const float q2 = __fdiv_rn(r1.hi, b.hi);
+  const df r2 = df_sub(r1, df_mul_f(b, q2));
+  const float q3 = __fdiv_rn(r2.hi, b.hi);
+  float s, e;
+  fast_two_sum(q1, q2, s, e);
+  return df_make(s, e + q3);
+}
+
+// sqrt(a) for a >= 0: the correctly rounded float32 root of the hi part and
+// one Newton correction from the exact remainder (~2^-46 relative).
+__device__ __forceinline__ df df_sqrt(df a) {
+  if (!(a.hi > 0.0f)) return df_make(0.0f, 0.0f);
+  const float x0 = __fsqrt_rn(a.hi);
+  float p, e;
+  two_prod(x0, x0, p, e);
+  const float r = ((a.hi - p) - e) + a.lo;
+  return df_make(x0, __fdiv_rn(r, 2.0f * x0));
+}
+
+__device__ __forceinline__ df df_dot3(const df *a, const df *b) {
+  return df_add(df_add(df_mul(a[0], b[0]), df_mul(a[1], b[1])),
+                df_mul(a[2], b[2]));
+}
+
 __host__ __device__ __forceinline__ double df_to_double(df a) {
   return (double)a.hi + (double)a.lo;
 }

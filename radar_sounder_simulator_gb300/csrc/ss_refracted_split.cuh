@@ -228,6 +228,108 @@ static __device__ __noinline__ void cell64(const ss_interface &I, const double *
   for (int j = 0; j < 3; ++j) x_out[j] = R.x[j];
 }
 
+// The float64 mean-plane solve of cell64 restated in double-float on the
+// FP32 pipe (GB300 runs float64 at 1/64 of the float32 rate): the same
+// projections, the same safeguarded Newton on sigma = sin(theta) from the
+// same start, ~2^-46 relative per operation, so the crossing agrees with
+// the float64 one to ~1e-10 m. Returns false if the last Newton step has
+// not settled below 1e-12 of sigma (the float64 chain then decides).
+// Out of line: only the fix-up runs it, and one copy of its long body keeps
+// that kernel's instruction footprint small.
+static __device__ __noinline__ bool snell_df(const df *p, const df *q,
+                                         const df *o, const df *nrm,
+                                         double n1, double n2, int n_iter,
+                                         df *x) {
+  const df tiny = df_make(1e-30f, 0.0f);
+  df po[3], qo[3];
+  for (int j = 0; j < 3; ++j) {
+    po[j] = df_sub(p[j], o[j]);
+    qo[j] = df_sub(q[j], o[j]);
+  }
+  const df h1 = df_dot3(po, nrm), h2 = df_dot3(qo, nrm);
+  const df a = df_abs(h1), b = df_abs(h2);
+  df fp[3], w[3];
+  for (int j = 0; j < 3; ++j) {
+    fp[j] = df_sub(p[j], df_mul(h1, nrm[j]));
+    w[j] = df_sub(df_sub(q[j], df_mul(h2, nrm[j])), fp[j]);
+  }
+  const df L = df_sqrt(df_dot3(w, w));
+  const df Lm = df_max(L, tiny);
+  df u[3];
+  for (int j = 0; j < 3; ++j) u[j] = df_div(w[j], Lm);
+  const df s = df_max(df_add(df_add(a, b), L), tiny);
+  const df ah = df_div(a, s), bh = df_div(b, s), Lh = df_div(L, s);
+  const bool swap = n1 > n2;
+  const df ratio = df_from_double(fmin(n1, n2) / fmax(n1, n2));
+  const df ar = swap ? bh : ah, bd = swap ? ah : bh;
+  const df one = df_make(1.0f, 0.0f);
+  const df hi0 = df_from_double(1.0 - 8.0 * kEps64);
+  const df abh = df_add(ah, bh);
+  df sig = df_min(df_div(Lh, df_max(df_sqrt(df_add(df_mul(Lh, Lh),
+                                                   df_mul(abh, abh))),
+                                    tiny)),
+                  hi0);
+  df lo = df_make(0.0f, 0.0f), hi = hi0;
+  float step = 1.0f;
+  for (int it = 0; it < n_iter; ++it) {
+    const df v = df_mul(ratio, sig);
+    const df c1 = df_max(df_mul(df_sub(one, sig), df_add(one, sig)), tiny);
+    const df c2 = df_max(df_mul(df_sub(one, v), df_add(one, v)), tiny);
+    const df sc1 = df_sqrt(c1), sc2 = df_sqrt(c2);
+    const df F = df_sub(df_add(df_div(df_mul(ar, sig), sc1),
+                               df_div(df_mul(bd, v), sc2)),
+                        Lh);
+    if (!(F.hi > 0.0f)) lo = sig; else hi = sig;
+    const df Fp = df_add(df_div(ar, df_mul(c1, sc1)),
+                         df_div(df_mul(bd, ratio), df_mul(c2, sc2)));
+    const df sn = df_sub(sig, df_div(F, df_max(Fp, tiny)));
+    const bool ok = !df_lt(sn, lo) && !df_lt(hi, sn) && isfinite(sn.hi);
+    const df nxt = ok ? sn : df_mul_f(df_add(lo, hi), 0.5f);
+    step = fabsf(df_sub(nxt, sig).hi);
+    sig = nxt;
+    if (step <= 1e-14f * fmaxf(sig.hi, 1e-12f)) break;
+  }
+  const df c1 = df_max(df_mul(df_sub(one, sig), df_add(one, sig)), tiny);
+  const df tr = df_div(df_mul(ar, sig), df_sqrt(c1));
+  const df t = df_min(df_max(swap ? df_sub(Lh, tr) : tr,
+                             df_make(0.0f, 0.0f)),
+                      Lh);
+  const df st = df_mul(s, t);
+  for (int j = 0; j < 3; ++j) x[j] = df_add(fp[j], df_mul(st, u[j]));
+  return step <= 1e-12f * fmaxf(sig.hi, 1e-12f);
+}
+
+// The reference's cell of a crossing from the double-float mean-plane solve
+// when its affine coordinates lie more than 1e-8 cells from a rounding
+// boundary (the two solves differ by ~1e-11 cells); false otherwise, and
+// the float64 chain (cell64) decides.
+__device__ __forceinline__ bool cell_df(const ss_interface &I, const df *cur,
+                                        const df *q, double n1, double n2,
+                                        df *x_out, int &row, int &col) {
+  df o[3], nrm[3], x[3];
+  for (int j = 0; j < 3; ++j) {
+    o[j] = df_from_double(I.mean_point[j]);
+    nrm[j] = df_from_double(I.mean_normal[j]);
+  }
+  if (!snell_df(cur, q, o, nrm, n1, n2, 10, x)) return false;
+  int idx[2];
+  for (int c = 0; c < 2; ++c) {
+    const df rc = df_add(df_add(df_mul(x[0], df_from_double(I.coef[c])),
+                                df_mul(x[1], df_from_double(I.coef[2 + c]))),
+                         df_from_double(I.coef[4 + c]));
+    // signed distance from the half between fl and fl + 1: the first
+    // difference is exact, so d carries rounding relative to itself only
+    const float fl = floorf(rc.hi);
+    const float d = (rc.hi - (fl + 0.5f)) + rc.lo;
+    if (fabsf(d) < 1e-8f) return false;
+    idx[c] = (int)(fl + (d > 0.0f ? 1.0f : 0.0f));
+  }
+  row = min(max(idx[0], 0), I.ny - 1);
+  col = min(max(idx[1], 0), I.nx - 1);
+  for (int j = 0; j < 3; ++j) x_out[j] = x[j];
+  return true;
+}
+
 // Plane point o and unit normal n of a table cell; t (optional) receives
 // the normal as stored, whose direction the float64 form uses.
 __device__ __forceinline__ void cell_plane32(const ss_interface &I, int row,
@@ -329,10 +431,22 @@ __device__ __forceinline__ void path_sequential_split(const RefArgs &a,
         P.defer = true;
         return;
       }
-      double cur64[3], q64[3] = {q[0], q[1], q[2]}, x1[3];
-      for (int j = 0; j < 3; ++j)
-        cur64[j] = i == 0 ? p64[j] : (double)o_prev[j] + (double)y_prev[j];
-      cell64(I, cur64, q64, a.n_leg[i], a.n_leg[i + 1], true, x1, row, col);
+      // the double-float solve decides unless the crossing is within
+      // 1e-8 cells of a boundary; then the float64 chain of the reference
+      df cdf[3], qdf[3], xdf[3];
+      for (int j = 0; j < 3; ++j) {
+        cdf[j] = i == 0 ? df_from_double(p64[j])
+                        : df_make(o_prev[j], 0.0f);
+        if (i > 0) cdf[j] = df_add_f(cdf[j], y_prev[j]);  // exact sum
+        qdf[j] = df_make(q[j], 0.0f);
+      }
+      if (!cell_df(I, cdf, qdf, a.n_leg[i], a.n_leg[i + 1], xdf, row, col)) {
+        double cur64[3], q64[3] = {q[0], q[1], q[2]}, x1[3];
+        for (int j = 0; j < 3; ++j)
+          cur64[j] = i == 0 ? p64[j] : (double)o_prev[j] + (double)y_prev[j];
+        cell64(I, cur64, q64, a.n_leg[i], a.n_leg[i + 1], true, x1, row,
+               col);
+      }
     }
     float o[3], n[3], tn[3];
     cell_plane32(I, row, col, o, n, tn);
@@ -434,11 +548,25 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
         P.defer = true;
         return;
       }
-      double c64[3] = {p64[0], p64[1], p64[2]};
-      const double q64[3] = {q[0], q[1], q[2]};
-      for (int i = 0; i < ni; ++i)
-        cell64(a.ifc[i], c64, q64, a.n_leg[i], a.n_leg[i + 1], false, c64,
-               rows[i], cols[i]);
+      // the double-float chain decides every cell unless a crossing is
+      // within 1e-8 cells of a boundary; then the float64 chain of the
+      // reference decides them all
+      df cdf[3], qdf[3];
+      for (int j = 0; j < 3; ++j) {
+        cdf[j] = df_from_double(p64[j]);
+        qdf[j] = df_make(q[j], 0.0f);
+      }
+      bool dfok = true;
+      for (int i = 0; i < ni && dfok; ++i)
+        dfok = cell_df(a.ifc[i], cdf, qdf, a.n_leg[i], a.n_leg[i + 1], cdf,
+                       rows[i], cols[i]);
+      if (!dfok) {
+        double c64[3] = {p64[0], p64[1], p64[2]};
+        const double q64[3] = {q[0], q[1], q[2]};
+        for (int i = 0; i < ni; ++i)
+          cell64(a.ifc[i], c64, q64, a.n_leg[i], a.n_leg[i + 1], false, c64,
+                 rows[i], cols[i]);
+      }
     }
   }
   // local planes and exact segment bases D_0 = o_0 - p, D_k = o_k - o_k-1,
@@ -1045,6 +1173,9 @@ refracted_split_kernel(RefArgs a, RefSplitConsts k) {
 // written in full. Deferred pairs are sparse (a few per thousand bits), so
 // each warp scans 32 mask words at a time and queues their set bits in
 // shared memory, then evaluates them 32 at a time with every lane busy.
+// 4 CTAs per SM (128 registers, a few hundred bytes of spills): the
+// fix-up is bound by instruction fetch over its long exact path, and twice
+// the resident warps (from 246 registers and two CTAs) hide more of it.
 constexpr int kFixWarps = 4;
 constexpr int kFixQueue = 32 * 32 + 32;  // one scan round plus a partial batch
 
@@ -1076,7 +1207,7 @@ __device__ __forceinline__ void fixup_pair(const RefArgs &a,
 }
 
 template <int NI, int ROUGH>
-__global__ void __launch_bounds__(32 * kFixWarps)
+__global__ void __launch_bounds__(32 * kFixWarps, 4)
 refracted_split_fixup(RefArgs a, RefSplitConsts k) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *lg = reinterpret_cast<float *>(smem_raw);
@@ -1248,7 +1379,7 @@ refracted_batch_kernel(const RefBatchJob *jobs, int n_jobs,
 // so each warp's 32-word scan belongs to one job; queued bits carry their
 // job. The jobs share one antenna table (staged once).
 template <int NI, int ROUGH>
-__global__ void __launch_bounds__(32 * kFixWarps)
+__global__ void __launch_bounds__(32 * kFixWarps, 4)
 refracted_batch_fixup(const RefBatchJob *jobs, int n_jobs,
                       long long n_words) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
