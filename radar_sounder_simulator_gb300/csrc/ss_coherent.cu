@@ -18,6 +18,7 @@
 
 #include "ss_internal.cuh"
 #include "ss_coherent.cuh"
+#include "ss_f32.cuh"
 
 namespace ss {
 
@@ -396,6 +397,15 @@ int build_co_args(const ss_coherent_opts *opts, const ss_facets *facets,
   a.pat_n = pattern ? pattern->n : 0;
   a.pa = pattern ? pattern->pa : nullptr;
   a.pb = pattern ? pattern->pb : nullptr;
+  if (a.precision == SS_PREC_SPLIT) {
+    // the split kernels stage the antenna table in shared memory
+    int pa_len, pb_len;
+    pattern_lengths(a.pat_kind, a.pat_n, pa_len, pb_len);
+    if (pa_len + pb_len > SS_PAT_MAX) {
+      set_error("antenna table too large for the split kernel");
+      return SS_ERR_UNSUPPORTED;
+    }
+  }
   if (a.pat_kind != SS_PAT_ISOTROPIC && (!traces->pv || traces->pv_len < 3)) {
     set_error("antenna pattern needs per-trace pattern vectors");
     return SS_ERR_ARG;

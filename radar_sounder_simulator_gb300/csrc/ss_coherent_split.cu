@@ -14,7 +14,11 @@
 //     products of q = p_c - c with the facet's normal and edge vectors.
 //   * Per trace t of the block, with w = p_t - p_c (a few trace spacings):
 //     r_t^2 - r_c^2 = 2 q.w + |w|^2 = N, so r_t - r_c = N / (r_c + r_t).
-//     N is a double-float (exact products, compensated sums), the division
+//     Within a block the track is straight to well under a metre, so
+//     w = lam u + eps with u the block's track direction: q.u is formed
+//     once per facet as a double-float, and N = 2 (lam q.u + q.eps) +
+//     |w|^2 takes one exact product per pair (q.eps, |eps| < 1 m, in
+//     float32). N is thus a double-float; the division
 //     takes a float32 quotient and one correction against the double-float
 //     denominator 2 r_c + dr, so dr = r_t - r_c is good to ~2e-11 of its
 //     size (3e-9 m at |w| = 160 m; a float32 dr would carry ulp(|w|)/2 of
@@ -27,9 +31,9 @@
 // bin (~1e-10 bins, FP32 pipe), and only within 1e-8 bins of an edge does
 // the float64 round-to-nearest chain of the oracle decide, so bins are
 // bit-identical to the float64 form while the slow FP64 pipe almost never
-// runs. A block whose traces lie more than 160 m from its middle trace
-// (sparse or crooked tracks) takes a reference per trace instead (w = 0
-// for every pair).
+// runs. A block whose traces lie more than 160 m from its middle trace or
+// more than 1 m off its straight track line (sparse or crooked tracks)
+// takes a reference per trace instead (w = 0 for every pair).
 //
 // Everything else (incidence, sincs, taper, antenna gain, roughness series)
 // runs in float32 from q + w and the facet's per-block products;
@@ -46,6 +50,9 @@ namespace ss {
 // Widest trace block (largest |p_t - p_c|, metres) served by one reference:
 // eight traces at 40 m.
 constexpr float kWideBlock = 160.0f;
+// Largest offset of a block's traces from its straight track line
+// (metres): q.eps is formed in float32, ~1e-3 |eps| m^2 of rounding.
+constexpr double kBlockBend = 1.0;
 // Bin-edge band of the per-trace bin position (~10x its error).
 constexpr float kBinBand = 2e-6f;
 
@@ -69,14 +76,19 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   float *him = hre + (size_t)a.tb * hs;
   __shared__ float s_ph[SS_MAX_TB][3], s_pl[SS_MAX_TB][3];
   __shared__ double s_p64[SS_MAX_TB][3];
-  __shared__ float4 s_w[SS_MAX_TB];   // p_t - p_c (hi), |p_t - p_c|^2
-  __shared__ float4 s_wl[SS_MAX_TB];  // p_t - p_c (lo), |p_t - p_c|^2 (lo)
-  __shared__ float s_wn[SS_MAX_TB];    // |p_t - p_c|
+  // trace offsets w = p_t - p_c = lam u + eps, u the block's track
+  // direction: w (float) and |w|^2 (hi), lam (hi, lo) and |w|^2 (lo), eps
+  __shared__ float4 s_w[SS_MAX_TB];
+  __shared__ float4 s_lw[SS_MAX_TB];
+  __shared__ float4 s_we[SS_MAX_TB];
+  __shared__ float s_tu[6];  // u as hi (3) and lo (3)
   __shared__ float s_u[SS_MAX_TB][3];
   __shared__ float s_pv[SS_MAX_TB][6];
   __shared__ int2 s_win[SS_MAX_TB];
   __shared__ float s_drop[SS_MAX_TB];
   __shared__ float s_pat[SS_PAT_MAX];
+  __shared__ float s_slope[SS_PAT_MAX / 2];  // tabulated pattern's slopes
+  __shared__ float s_tinv;
   __shared__ float s_fad[SS_FAD_N];
   __shared__ int s_rng[2];
   __shared__ int s_next;
@@ -102,12 +114,9 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       w[j] = pj - a.pos[3 * tc + j];
       w2 += w[j] * w[j];
     }
-    const float wx = (float)w[0], wy = (float)w[1], wz = (float)w[2];
     const float w2h = (float)w2;
-    s_w[tid] = make_float4(wx, wy, wz, w2h);
-    s_wl[tid] = make_float4((float)(w[0] - wx), (float)(w[1] - wy),
-                            (float)(w[2] - wz), (float)(w2 - (double)w2h));
-    s_wn[tid] = (float)sqrt(w2);
+    s_w[tid] = make_float4((float)w[0], (float)w[1], (float)w[2], w2h);
+    s_lw[tid].z = (float)(w2 - (double)w2h);
     for (int j = 0; j < 6; ++j)
       s_pv[tid][j] =
           (a.pv && j < a.pv_len) ? (float)a.pv[a.pv_len * t + j] : 0.0f;
@@ -123,19 +132,54 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
     s_fad[tid] = (float)a.fad.a[tid];
   for (int j = tid; j < 2 * a.tb * hs; j += blockDim.x) hre[j] = 0.0f;
   __syncthreads();
+  if (a.pat_kind == SS_PAT_TABULATED)
+    tab_slopes(a.pat_n, s_pat, s_pat + pa_len, s_slope, &s_tinv, tid,
+               blockDim.x);
   if (tid == 0) {
     int lo = s_win[0].x, hi = s_win[0].y;
-    float wmax = s_wn[0];
     for (int j = 1; j < nt; ++j) {
       lo = min(lo, s_win[j].x);
       hi = max(hi, s_win[j].y);
-      wmax = fmaxf(wmax, s_wn[j]);
     }
     long len = max(hi - lo, 0);
     s_rng[0] = lo + (int)(len * chunk / a.n_chunks);
     s_rng[1] = lo + (int)(len * (chunk + 1) / a.n_chunks);
     s_next = s_rng[0];
-    s_ref = wmax <= kWideBlock ? nt / 2 : -1;
+    // track direction u of the block (first to last trace) and each
+    // trace's offset w = lam u + eps from the middle trace, in float64
+    const int c = nt / 2;
+    double u[3], un = 0.0;
+    for (int j = 0; j < 3; ++j) {
+      u[j] = s_p64[nt - 1][j] - s_p64[0][j];
+      un += u[j] * u[j];
+    }
+    un = sqrt(un);
+    for (int j = 0; j < 3; ++j) u[j] = un > 0.0 ? u[j] / un : (j == 0);
+    double wmax = 0.0, emax = 0.0;
+    for (int t = 0; t < nt; ++t) {
+      double w[3], lam = 0.0, e2 = 0.0;
+      for (int j = 0; j < 3; ++j) {
+        w[j] = s_p64[t][j] - s_p64[c][j];
+        lam += w[j] * u[j];
+      }
+      float e[3];
+      for (int j = 0; j < 3; ++j) {
+        const double ej = w[j] - lam * u[j];
+        e[j] = (float)ej;
+        e2 += ej * ej;
+      }
+      const float lh = (float)lam;
+      s_lw[t].x = lh;
+      s_lw[t].y = (float)(lam - (double)lh);
+      s_we[t] = make_float4(e[0], e[1], e[2], 0.0f);
+      wmax = fmax(wmax, sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]));
+      emax = fmax(emax, sqrt(e2));
+    }
+    for (int j = 0; j < 3; ++j) {
+      s_tu[j] = (float)u[j];
+      s_tu[3 + j] = (float)(u[j] - (double)s_tu[j]);
+    }
+    s_ref = wmax <= kWideBlock && emax <= kBlockBend ? c : -1;
   }
   __syncthreads();
 
@@ -181,6 +225,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
     // --- per-facet reference at the platform of trace `j` ---
     float qhx, qhy, qhz, qlx, qly, qlz, rch, phc, ubc, fc, cosc, qe1, qe2;
     float rcl, xnx = 0.f, xny = 0.f, xnz = 0.f;  // q x n (taper's sin^2)
+    float quh, qul;                               // q.u as a double-float
     auto reference = [&](int j) {
       float e;
       two_sum(s_ph[j][0], -cx, qhx, e);
@@ -236,6 +281,19 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
         xnx = __fmaf_rn(qhy, nz, -qhz * ny) + __fmaf_rn(qly, nz, -qlz * ny);
         xny = __fmaf_rn(qhz, nx, -qhx * nz) + __fmaf_rn(qlz, nx, -qlx * nz);
         xnz = __fmaf_rn(qhx, ny, -qhy * nx) + __fmaf_rn(qlx, ny, -qly * nx);
+      }
+      // q.u (u the block's track direction) as a double-float
+      {
+        float p1, e1, p2, e2, p3, e3, s1, f1, s2, f2;
+        two_prod(qhx, s_tu[0], p1, e1);
+        two_prod(qhy, s_tu[1], p2, e2);
+        two_prod(qhz, s_tu[2], p3, e3);
+        two_sum(p1, p2, s1, f1);
+        two_sum(s1, p3, s2, f2);
+        const float l = (f1 + f2) + (e1 + e2 + e3) +
+                        dot3f(qlx, qly, qlz, s_tu[0], s_tu[1], s_tu[2]) +
+                        dot3f(qhx, qhy, qhz, s_tu[3], s_tu[4], s_tu[5]);
+        fast_two_sum(s2, l, quh, qul);
       }
       // products with the edge vectors (q_lo matters for the sinc
       // arguments: k (r_hat . e) reaches tens of radians)
@@ -299,25 +357,20 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       frac = fr2;
     };
 
-    // --- one pair: facet i, trace tt at offset w (hi, |w|^2) + wl (lo) ---
-    auto pair = [&](int tt, float4 w, float4 wl) -> float {
-      // N = r_t^2 - r_c^2 = 2 q.w + |w|^2 as a double-float: exact
-      // products of the hi parts, compensated sums, the lo parts' products
-      // (q_lo.w_hi + q_hi.w_lo) and |w|^2's lo part in float
-      float p1, e1, p2, e2, p3, e3, s1, f1, s2, f2;
-      two_prod(qhx, w.x, p1, e1);
-      two_prod(qhy, w.y, p2, e2);
-      two_prod(qhz, w.z, p3, e3);
-      two_sum(p1, p2, s1, f1);
-      two_sum(s1, p3, s2, f2);
-      const float corr = __fmaf_rn(
-          qhx, wl.x, __fmaf_rn(qhy, wl.y, __fmaf_rn(
-              qhz, wl.z, __fmaf_rn(qlx, w.x, __fmaf_rn(qly, w.y,
-                                                       qlz * w.z)))));
-      const float lo = (f1 + f2) + (e1 + e2 + e3) + corr;
+    // --- one pair: facet i, trace tt at offset w = lam u + eps ---
+    auto pair = [&](int tt, float4 w, float4 lw, float4 we) -> float {
+      // N = r_t^2 - r_c^2 = 2 q.w + |w|^2 as a double-float, with
+      // q.w = lam (q.u) + q.eps: one exact product of the hi parts, the lo
+      // parts' products and q.eps (|eps| < 1 m) in float
+      float pq, eq;
+      two_prod(lw.x, quh, pq, eq);
+      const float lo = eq + __fmaf_rn(lw.x, qul, lw.y * quh) +
+                       dot3f(qhx, qhy, qhz, we.x, we.y, we.z);
+      // (2 lo + |w|^2 can reach 4e4 m^2 on a bent block: it joins the
+      // compensated sum, so N comes out renormalised)
       float Nh, g;
-      two_sum(2.0f * s2, w.w, Nh, g);
-      const float Nl = g + __fmaf_rn(2.0f, lo, wl.w);
+      two_sum(2.0f * pq, __fmaf_rn(2.0f, lo, w.w), Nh, g);
+      const float Nl = g + lw.z;
       // float32 r_t for the amplitude and a first dr, then dr = N / D with
       // D = r_c + r_t = 2 r_c + dr as a double-float and one correction:
       // dr is then good to ~2e-11 of its size
@@ -378,7 +431,12 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       float im = cr * cs + ci * sn;
       const float qtx = qhx + w.x, qty = qhy + w.y, qtz = qhz + w.z;
       if (a.pat_kind != SS_PAT_ISOTROPIC) {
-        const float g = gain32(a.pat_kind, a.pat_n, pa_len, s_pat, s_pv[tt],
+        const float g =
+            a.pat_kind == SS_PAT_TABULATED
+                ? gain_tab32(a.pat_n, s_pat, s_pat + pa_len, s_slope, s_tinv,
+                             s_pv[tt], -qtx * inv_r, -qty * inv_r,
+                             -qtz * inv_r)
+                : gain32(a.pat_kind, a.pat_n, pa_len, s_pat, s_pv[tt],
                                -qtx * inv_r, -qty * inv_r, -qtz * inv_r);
         re *= g * g;
         im *= g * g;
@@ -432,7 +490,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
         const int tt = rot + st < nt ? rot + st : rot + st - nt;
         const int2 win = s_win[tt];
         if (i >= win.x && i < win.y) {
-          const float d = pair(tt, s_w[tt], s_wl[tt]);
+          const float d = pair(tt, s_w[tt], s_lw[tt], s_we[tt]);
           if (d != 0.0f) dropl[st] += d;
         }
       }
@@ -441,8 +499,8 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
         const int2 win = s_win[tt];
         if (i < win.x || i >= win.y) continue;
         reference(tt);
-        const float d = pair(tt, make_float4(0.f, 0.f, 0.f, 0.f),
-                             make_float4(0.f, 0.f, 0.f, 0.f));
+        const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float d = pair(tt, z, z, z);
         if (d != 0.0f) atomicAdd(&s_drop[tt], d);
       }
     }

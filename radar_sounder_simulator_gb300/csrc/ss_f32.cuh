@@ -134,6 +134,35 @@ __device__ __forceinline__ float gain32(int kind, int n, int pa_len,
   }
 }
 
+// The tabulated kind of gain32 with its per-segment slopes and index scale
+// staged once per CTA (`slope[j]` = the same quotient gain32 forms for
+// segment j, `inv` = (n - 1) / span): the same operations on the same
+// values, so the same gain bit for bit.
+__device__ __forceinline__ void tab_slopes(int n, const float *pa,
+                                           const float *pb, float *slope,
+                                           float *inv, int tid, int nthr) {
+  for (int j = tid; j < n - 1; j += nthr)
+    slope[j] = __fdividef(pb[j + 1] - pb[j], pa[j + 1] - pa[j]);
+  if (tid == 0) *inv = __fdividef((float)(n - 1), pa[n - 1] - pa[0]);
+}
+
+__device__ __forceinline__ float gain_tab32(int n, const float *pa,
+                                            const float *pb,
+                                            const float *slope, float inv,
+                                            const float *pv, float dx,
+                                            float dy, float dz) {
+  float ct = fminf(fmaxf(dot3f(dx, dy, dz, pv[0], pv[1], pv[2]), -1.0f),
+                   1.0f);
+  float th = acosf(ct);
+  if (th <= pa[0]) return pb[0];
+  if (th >= pa[n - 1]) return pb[n - 1];
+  int lo = (int)((th - pa[0]) * inv);
+  lo = min(max(lo, 0), n - 2);
+  while (lo < n - 2 && pa[lo + 1] <= th) ++lo;
+  while (lo > 0 && pa[lo] > th) --lo;
+  return __fmaf_rn(slope[lo], th - pa[lo], pb[lo]);
+}
+
 // Weideman w(z) in float32 (roughness.py:67-80).
 __device__ __forceinline__ void faddeeva32(const float *a, float L, float zr,
                                            float zi, float &wr, float &wi) {

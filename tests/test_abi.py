@@ -178,3 +178,34 @@ def test_missing_library_fails_loudly(monkeypatch, tmp_path):
                             device="cpu")
     with pytest.raises(_lib.LibraryMissing):
         plan.run()
+
+
+def test_split_jobs_refuse_antenna_tables_above_shared_capacity():
+    """The split kernels stage the antenna table in shared memory (up to
+    256 floats: 128 samples of a tabulated pattern). A larger table is
+    refused while the job is validated -- for the one-call and the batched
+    entry points alike -- before any device work (the pointers here are
+    placeholders that are never dereferenced)."""
+    import ctypes as C
+    L = _lib.lib()
+    buf = (C.c_double * 4)()
+    ptr = C.cast(buf, C.c_void_p)
+    job = _lib.CoherentJob()
+    job.opts.k, job.opts.c, job.opts.dt = 1.0, 3e8, 1e-8
+    job.opts.n_samples, job.opts.block_size, job.opts.n_win = 64, 64, 1
+    job.opts.precision = _lib.PREC["split"]
+    job.facets.cx = job.facets.area = ptr
+    job.facets.n_facets = 64
+    job.traces.pos = job.traces.off = job.traces.pv = ptr
+    job.traces.n_traces, job.traces.pv_len = 4, 3
+    job.pattern.kind = 5  # SS_PAT_TABULATED
+    job.pattern.pa = job.pattern.pb = ptr
+    job.out.field_c128 = job.out.dropped = ptr
+    for n, ok in ((128, True), (129, False)):
+        job.pattern.n = n
+        got = L.ss_coherent_batch_scratch_bytes(C.byref(job), 1, None)
+        if ok:
+            assert got > 0
+        else:
+            assert got == 0
+            assert "antenna table too large" in L.ss_last_error().decode()
