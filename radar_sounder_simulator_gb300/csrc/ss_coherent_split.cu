@@ -538,9 +538,12 @@ coherent_split_kernel(CoArgs a, SplitConsts k) {
 
 // Batched persistent kernel: CTAs pull (job, trace block, facet chunk)
 // items from a global counter until the queue is empty, so jobs of very
-// different sizes share one launch without tail effects.
-template <int ROUGH>
-__global__ void __launch_bounds__(SS_SPLIT_MAXT(ROUGH), SS_SPLIT_MINB(ROUGH))
+// different sizes share one launch without tail effects. Two builds:
+// MAXT = 512 (smooth facets only, 64 registers, two CTAs per SM) and
+// MAXT = 256 (80 registers, three CTAs per SM, no spills); the batch's CTA
+// size picks one, and the autotuner times both.
+template <int ROUGH, int MAXT>
+__global__ void __launch_bounds__(MAXT, MAXT == 512 ? 2 : 3)
 coherent_batch_split_kernel(const BatchJob *jobs, int n_jobs,
                             long long n_items, unsigned long long *counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -563,16 +566,27 @@ coherent_batch_split_kernel(const BatchJob *jobs, int n_jobs,
   }
 }
 
+// The build of the batch kernel for a CTA size (512 only for smooth
+// facets, which the batch layout enforces).
 template <int ROUGH>
-static int batch_split_launch_r(const BatchJob *jobs, int n_jobs,
-                                long long n_items,
-                                unsigned long long *counter, int threads,
-                                int ctas, size_t smem, cudaStream_t st) {
-  // the dynamic shared-memory limit was raised at prepare time, so this
-  // path holds only stream operations (it may run under graph capture)
-  coherent_batch_split_kernel<ROUGH><<<ctas, threads, smem, st>>>(
-      jobs, n_jobs, n_items, counter);
-  return cuda_status(cudaGetLastError(), "batch split launch");
+static void *batch_split_fn(int threads) {
+  if constexpr (ROUGH == SS_ROUGH_NONE) {
+    if (threads > 256)
+      return reinterpret_cast<void *>(
+          coherent_batch_split_kernel<ROUGH, 512>);
+  }
+  return reinterpret_cast<void *>(coherent_batch_split_kernel<ROUGH, 256>);
+}
+
+static void *batch_split_fn_kind(int rough_kind, int threads) {
+  switch (rough_kind) {
+    case SS_ROUGH_NONE: return batch_split_fn<SS_ROUGH_NONE>(threads);
+    case SS_ROUGH_GAUSS_FULL:
+      return batch_split_fn<SS_ROUGH_GAUSS_FULL>(threads);
+    case SS_ROUGH_GAUSS_AREA:
+      return batch_split_fn<SS_ROUGH_GAUSS_AREA>(threads);
+    default: return batch_split_fn<SS_ROUGH_EXP_AREA>(threads);
+  }
 }
 
 int coherent_batch_split_launch(const BatchJob *jobs, int n_jobs,
@@ -580,49 +594,28 @@ int coherent_batch_split_launch(const BatchJob *jobs, int n_jobs,
                                 unsigned long long *counter, int rough_kind,
                                 int threads, int ctas, size_t smem,
                                 cudaStream_t st) {
-  switch (rough_kind) {
-    case SS_ROUGH_NONE:
-      return batch_split_launch_r<SS_ROUGH_NONE>(jobs, n_jobs, n_items,
-                                                 counter, threads, ctas, smem,
-                                                 st);
-    case SS_ROUGH_GAUSS_FULL:
-      return batch_split_launch_r<SS_ROUGH_GAUSS_FULL>(
-          jobs, n_jobs, n_items, counter, threads, ctas, smem, st);
-    case SS_ROUGH_GAUSS_AREA:
-      return batch_split_launch_r<SS_ROUGH_GAUSS_AREA>(
-          jobs, n_jobs, n_items, counter, threads, ctas, smem, st);
-    default:
-      return batch_split_launch_r<SS_ROUGH_EXP_AREA>(
-          jobs, n_jobs, n_items, counter, threads, ctas, smem, st);
-  }
+  // the dynamic shared-memory limit was raised at prepare time, so this
+  // path holds only stream operations (it may run under graph capture)
+  void *fn = batch_split_fn_kind(rough_kind, threads);
+  void *args[] = {(void *)&jobs, (void *)&n_jobs, (void *)&n_items,
+                  (void *)&counter};
+  return cuda_status(cudaLaunchKernel(fn, dim3(ctas), dim3(threads), args,
+                                      smem, st),
+                     "batch split launch");
 }
 
 int batch_split_blocks_per_sm(int rough_kind, int threads, size_t smem) {
   // raise the kernel's dynamic shared-memory limit to the largest size any
   // prepared batch uses (never lowered: earlier batches stay launchable)
-  static size_t limit[4] = {0, 0, 0, 0};
-  const int r = rough_kind & 3;
+  static size_t limit[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const int r = (rough_kind & 3) * 2 + (threads > 256 ? 1 : 0);
   limit[r] = std::max(limit[r], smem);
-  const int lim = (int)limit[r];
+  void *fn = batch_split_fn_kind(rough_kind, threads);
   int n = 0;
-  cudaError_t e = cudaSuccess;
-  switch (rough_kind) {
-#define SS_OCC(R)                                                            \
-  case R:                                                                    \
-    e = cudaFuncSetAttribute(coherent_batch_split_kernel<R>,                 \
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,    \
-                             lim);                                           \
-    if (e == cudaSuccess)                                                    \
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(                     \
-          &n, coherent_batch_split_kernel<R>, threads, smem);                \
-    break;
-    SS_OCC(SS_ROUGH_NONE)
-    SS_OCC(SS_ROUGH_GAUSS_FULL)
-    SS_OCC(SS_ROUGH_GAUSS_AREA)
-    default:
-      SS_OCC(SS_ROUGH_EXP_AREA)
-#undef SS_OCC
-  }
+  cudaError_t e = cudaFuncSetAttribute(
+      fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit[r]);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem);
   return e == cudaSuccess ? n : 0;
 }
 
