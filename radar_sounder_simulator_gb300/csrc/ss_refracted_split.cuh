@@ -528,8 +528,10 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   const int ni = NI == kDeepNI ? a.ni : NI;
   const float *nm = k.n_leg;
   P.defer = false;
-  // pass 1: mean-plane chain anchors the lookups
+  // pass 1: mean-plane chain anchors the lookups; its crossings (relative
+  // to each mean point) also seed the joint solve
   int rows[NI], cols[NI];
+  float Xm[NI][3];
   {
     float Pm[3] = {T.pm0[0], T.pm0[1], T.pm0[2]};
     bool safe = true;
@@ -541,7 +543,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
       Solve32 S;
       snell_rel32(Pm, Qm, M.mn, nm[i], nm[i + 1], 10, S);
       safe = cell_of(M, a.ifc[i], S.y, rows[i], cols[i]) && safe;
-      for (int j = 0; j < 3; ++j) Pm[j] = S.y[j];
+      for (int j = 0; j < 3; ++j) Pm[j] = Xm[i][j] = S.y[j];
     }
     if (!safe) {  // the reference's float64 chain for this pair
       if (!EXACT) {
@@ -590,25 +592,19 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   float Ds[NI + 1][3];
   for (int i = 0; i <= ni; ++i)
     for (int j = 0; j < 3; ++j) Ds[i][j] = D[i][j].hi * inv;
-  // chain initialiser (25 iterations), offsets y_i from o_i (scaled)
+  // Start of the joint solve: the mean-plane crossings of pass 1 moved onto
+  // the looked-up facet planes (offsets y_i from o_i, scaled). They lie
+  // within the facets' height and tilt from the mean planes -- tens of
+  // metres, ~1e-3 of the path scale -- so Gauss-Newton converges in the
+  // same few steps as from the reference's chain of two-point solves,
+  // whose three float32 solves it saves; the root is the same.
   float Y[NI][3];
-  {
-    float Qrel[NI][3];  // q - o_i = sum_{j > i} D_j
-    for (int j = 0; j < 3; ++j) {
-      float acc = Ds[ni][j];
-      for (int i = ni - 1; i >= 0; --i) {
-        Qrel[i][j] = acc;
-        acc += Ds[i][j];
-      }
-    }
-    for (int i = 0; i < ni; ++i) {
-      float Pr[3];
-      for (int j = 0; j < 3; ++j)
-        Pr[j] = i == 0 ? -Ds[0][j] : Y[i - 1][j] - Ds[i][j];
-      Solve32 S;
-      snell_rel32(Pr, Qrel[i], Nn[i], nm[i], nm[i + 1], 25, S);
-      for (int j = 0; j < 3; ++j) Y[i][j] = S.y[j];
-    }
+  for (int i = 0; i < ni; ++i) {
+    const float *mp = k.mean[i].mp;
+    for (int j = 0; j < 3; ++j)
+      Y[i][j] = ((mp[j] - O[i][j]) + Xm[i][j]) * inv;
+    const float yn = dot3a(Y[i], Nn[i]);
+    for (int j = 0; j < 3; ++j) Y[i][j] -= yn * Nn[i][j];
   }
   // in-plane bases and offsets
   float B[NI][3][2], ab[NI][2];
