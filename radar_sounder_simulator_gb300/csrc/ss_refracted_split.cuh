@@ -97,10 +97,12 @@ __device__ __forceinline__ float dot3a(const float *a, const float *b) {
 // resolution.
 __device__ __forceinline__ float sigma32(float ar, float bd, float Lh,
                                          float ah, float bh, float ratio,
-                                         int n_iter) {
+                                         int n_iter, float sig0 = -1.0f) {
   const float hi0 = 1.0f - 8.0f * kEps32;
-  float sig = fminf(Lh / fmaxf(sqrtf(Lh * Lh + (ah + bh) * (ah + bh)),
-                               kTiny32), hi0);
+  float sig = sig0 >= 0.0f
+                  ? fminf(sig0, hi0)
+                  : fminf(Lh / fmaxf(sqrtf(Lh * Lh + (ah + bh) * (ah + bh)),
+                                     kTiny32), hi0);
   float lo = 0.0f, hi = hi0;
   for (int it = 0; it < n_iter; ++it) {
     const float v = ratio * sig;
@@ -128,10 +130,14 @@ struct Solve32 {
   bool sides;    // end points strictly on opposite sides of the plane
 };
 
+// `x0` (optional, relative to the plane point): a point near the crossing
+// whose offset along the plane starts the Newton iteration on sigma in
+// place of the straight-line guess (the root is the same).
 __device__ __forceinline__ void snell_rel32(const float *P, const float *Q,
                                             const float *nrm, float n1,
                                             float n2, int n_iter,
-                                            Solve32 &S) {
+                                            Solve32 &S,
+                                            const float *x0 = nullptr) {
   const float h1 = dot3a(P, nrm), h2 = dot3a(Q, nrm);
   const float a = fabsf(h1), b = fabsf(h2);
   float fp[3], fq[3], w[3];
@@ -148,7 +154,18 @@ __device__ __forceinline__ void snell_rel32(const float *P, const float *Q,
   const bool swap = n1 > n2;
   const float ratio = fminf(n1, n2) / fmaxf(n1, n2);
   const float ar = swap ? bh : ah, bd = swap ? ah : bh;
-  const float sig = sigma32(ar, bd, Lh, ah, bh, ratio, n_iter);
+  float sig0 = -1.0f;
+  if (x0) {
+    // x0's offset from p's foot along w, normalised like tp, then the
+    // rare-side offset tr and sigma = tr / sqrt(ar^2 + tr^2)
+    const float tp0 = fminf(fmaxf(((x0[0] - fp[0]) * w[0] +
+                                   (x0[1] - fp[1]) * w[1] +
+                                   (x0[2] - fp[2]) * w[2]) * iL * inv_s,
+                                  0.0f), Lh);
+    const float tr0 = swap ? Lh - tp0 : tp0;
+    sig0 = tr0 * rsqrtf(fmaxf(ar * ar + tr0 * tr0, kTiny32));
+  }
+  const float sig = sigma32(ar, bd, Lh, ah, bh, ratio, n_iter, sig0);
   const float v = ratio * sig;
   const float tr = ar * sig * rsqrtf(fmaxf((1.0f - sig) * (1.0f + sig),
                                            kTiny32));
@@ -460,8 +477,13 @@ __device__ __forceinline__ void path_sequential_split(const RefArgs &a,
     for (int j = 0; j < 3; ++j) Qd[j] = df_diff(q[j], o[j]);
     const float Ph[3] = {Pd[0].hi, Pd[1].hi, Pd[2].hi};
     const float Qh[3] = {Qd[0].hi, Qd[1].hi, Qd[2].hi};
+    // the mean-plane crossing relative to this facet's plane point starts
+    // the local solve
+    const float x0[3] = {(M.mp[0] - o[0]) + Sm.y[0],
+                         (M.mp[1] - o[1]) + Sm.y[1],
+                         (M.mp[2] - o[2]) + Sm.y[2]};
     Solve32 S;
-    snell_rel32(Ph, Qh, n, k.n_leg[i], k.n_leg[i + 1], 25, S);
+    snell_rel32(Ph, Qh, n, k.n_leg[i], k.n_leg[i + 1], 25, S, x0);
     P.valid = P.valid && S.sides && fabsf(S.res) <= kTol32;
     for (int j = 0; j < 3; ++j) y[j] = S.y[j];
     // upper leg |cur - x| = |(cur - o) - y|
