@@ -426,7 +426,9 @@ typedef struct {
 
 /* Work decomposition of a batch (0 = default). */
 typedef struct {
-  int32_t threads;       /* CTA size: 128 or 256 (default 256) */
+  int32_t threads;       /* CTA size: 128 or 256 (default 256), or 512 for
+                            smooth split-precision coherent batches;
+                            refracted batches take 512 only */
   int32_t max_tb;        /* traces per work item, 1..8 (default 8) */
   int32_t items_per_sm;  /* work items per SM; sets facet-chunk sizes
                             (default 16) */
