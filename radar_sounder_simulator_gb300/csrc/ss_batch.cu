@@ -112,11 +112,11 @@ static int batch_layout(const ss_coherent_job *jobs, int n_jobs,
     off += align256((size_t)J.n_chunks * a.T * a.n_seg * elt);
     a.part_drop = reinterpret_cast<double *>(off);
     off += align256((size_t)J.n_chunks * a.T * sizeof(double));
-    // the FP64 kernel stages log-factorials of the series; the split kernel
-    // anchors its Poisson weights without a table
-    const size_t lg = a.rough_kind && a.precision == SS_PREC_FP64
-                          ? (size_t)(a.n_terms + 1) * 8
-                          : 0;
+    // the series table: log-factorials (FP64 kernel, doubles) or 1/m
+    // (split kernel, floats)
+    const size_t lg = a.rough_kind ? (size_t)(a.n_terms + 1) *
+                                         (a.precision == SS_PREC_FP64 ? 8 : 4)
+                                   : 0;
     const size_t hist = a.precision == SS_PREC_FP64
                             ? (size_t)a.tb * a.n_seg * elt
                             : split_hist_bytes(a.n_seg, a.tb);

@@ -74,6 +74,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   const int hs = split_hist_stride(a.n_seg);
   float *hre = reinterpret_cast<float *>(smem_raw);
   float *him = hre + (size_t)a.tb * hs;
+  float *inv = him + (size_t)a.tb * hs;  // 1/m of the series (rough only)
   __shared__ float s_ph[SS_MAX_TB][3], s_pl[SS_MAX_TB][3];
   __shared__ double s_p64[SS_MAX_TB][3];
   // trace offsets w = p_t - p_c = lam u + eps, u the block's track
@@ -131,6 +132,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
   if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
     s_fad[tid] = (float)a.fad.a[tid];
   for (int j = tid; j < 2 * a.tb * hs; j += blockDim.x) hre[j] = 0.0f;
+  if (ROUGH != SS_ROUGH_NONE) fill_inv_table(inv, a.n_terms, tid, blockDim.x);
   __syncthreads();
   if (a.pat_kind == SS_PAT_TABULATED)
     tab_slopes(a.pat_n, s_pat, s_pat + pa_len, s_slope, &s_tinv, tid,
@@ -407,7 +409,7 @@ __device__ __forceinline__ void coherent_split_cta(const CoArgs &a,
       float cr = amp, ci = 0.0f;
       if (ROUGH != SS_ROUGH_NONE) {
         const float kk = 2.0f * k.k * cosv;
-        const float dp = d_phi32<ROUGH>(a.n_terms, nullptr, s_fad, k.fadL,
+        const float dp = d_phi32<ROUGH>(a.n_terms, inv, s_fad, k.fadL,
                                         sg, lc, kk, 2.0f * k.k * d1 / l1,
                                         2.0f * k.k * d2 / l2, l1, l2);
         const float amp_i = area > 0.0f ? k.amp_pref * gam * cosv * inv_r2 *
@@ -649,7 +651,8 @@ int coherent_split_launch(CoArgs &a, const Plan &p, cudaStream_t st) {
   }
   const SplitConsts k = coherent_split_consts(a);
   dim3 grid(p.n_chunks, p.n_groups);
-  size_t smem = split_hist_bytes(a.n_seg, p.tb);
+  size_t smem = split_hist_bytes(a.n_seg, p.tb) +
+                (a.rough_kind ? (size_t)(a.n_terms + 1) * sizeof(float) : 0);
   cudaError_t e = cudaSuccess;
   switch (a.rough_kind) {
 #define SS_LAUNCH(R)                                                         \

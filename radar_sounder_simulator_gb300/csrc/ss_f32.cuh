@@ -246,16 +246,25 @@ __device__ __forceinline__ float poisson_anchor(int m, float x) {
   return expf(lp);
 }
 
+// 1/m for m = 1..n (t[0] = 0), correctly rounded, staged by the CTA for the
+// series: the reciprocal per term is then a shared-memory load instead of
+// a MUFU operation (the rough kernels are bound by that pipe).
+__device__ __forceinline__ void fill_inv_table(float *t, int n, int tid,
+                                               int nthr) {
+  for (int m = tid; m <= n; m += nthr)
+    t[m] = m ? __frcp_rn((float)m) : 0.0f;
+}
+
 // D_Phi in float32. Poisson weights are exact (poisson_anchor) at the start
 // of every run of 64 terms and follow the recursion P_m = P_(m-1) x / m
 // inside it (a few roundings per step, ~1e-6 relative at a run's end).
+// `inv`: the CTA's 1/m table (fill_inv_table) up to n_terms, or null.
 template <int KIND>
-__device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
+__device__ __forceinline__ float d_phi32(int n_terms, const float *inv,
                                          const float *fa, float fL,
                                          float sigma, float l, float K,
                                          float A0, float B0, float Lx,
                                          float Ly) {
-  (void)lg;
   const float sk = sigma * K;
   const float x = sk * sk;
   if (!(x > 0.0f)) return 0.0f;
@@ -270,14 +279,14 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
     for (int m0 = m_lo; m0 <= m_hi; m0 += 64) {
       float mf = (float)m0;
       float P = poisson_anchor(m0, x);
-      float im = __fdividef(1.0f, mf);
+      float im = inv ? inv[m0] : __fdividef(1.0f, mf);
       float im2 = im * im;
       float rs = rsqrtf(__fmaf_rn(kl2, im2, 1.0f));
       acc = __fmaf_rn(P * im2, rs * rs * rs, acc);
       const int m_end = min(m_hi, m0 + 63);
       for (int m = m0 + 1; m <= m_end; ++m) {
         mf += 1.0f;
-        im = __fdividef(1.0f, mf);
+        im = inv ? inv[m] : __fdividef(1.0f, mf);
         P *= x * im;
         im2 = im * im;
         rs = rsqrtf(__fmaf_rn(kl2, im2, 1.0f));
@@ -293,7 +302,7 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
       const int m_end = min(m_hi, m0 + 63);
       for (int m = m0; m <= m_end; ++m) {
         const float mf = (float)m;
-        const float im = __fdividef(1.0f, mf);
+        const float im = inv ? inv[m] : __fdividef(1.0f, mf);
         if (m > m0) P *= x * im;
         acc = __fmaf_rn(P * __expf(-c * im), im, acc);
       }
@@ -322,12 +331,11 @@ __device__ __forceinline__ float d_phi32(int n_terms, const float *lg,
 // itself (the form sum m P W / x - D cancels to ~1/sqrt(x) of its terms
 // near the Poisson peak). Same anchored Poisson weights as d_phi32.
 template <int KIND>
-__device__ __forceinline__ float d_phi32_dx(int n_terms, const float *lg,
+__device__ __forceinline__ float d_phi32_dx(int n_terms, const float *inv,
                                             const float *fa, float fL,
                                             float sigma, float l, float K,
                                             float A0, float B0, float Lx,
                                             float Ly, float &dDdx) {
-  (void)lg;
   dDdx = 0.0f;
   const float sk = sigma * K;
   const float x = sk * sk;
@@ -343,7 +351,7 @@ __device__ __forceinline__ float d_phi32_dx(int n_terms, const float *lg,
       float P = poisson_anchor(m0, x);
       const int m_end = min(m_hi, m0 + 63);
       for (int m = m0; m <= m_end; ++m) {
-        const float im = __fdividef(1.0f, mf);
+        const float im = inv ? inv[m] : __fdividef(1.0f, mf);
         if (m > m0) P *= x * im;
         const float im2 = im * im;
         const float rs = rsqrtf(__fmaf_rn(kl2, im2, 1.0f));
@@ -362,7 +370,7 @@ __device__ __forceinline__ float d_phi32_dx(int n_terms, const float *lg,
       const int m_end = min(m_hi, m0 + 63);
       for (int m = m0; m <= m_end; ++m) {
         const float mf = (float)m;
-        const float im = __fdividef(1.0f, mf);
+        const float im = inv ? inv[m] : __fdividef(1.0f, mf);
         if (m > m0) P *= x * im;
         float t;
         if (KIND == SS_ROUGH_GAUSS_AREA) {

@@ -143,9 +143,7 @@ multifreq_split_kernel(MfArgs a, MfSplitConsts k) {
   }
   if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
     s_fad[tid] = (float)a.fad.a[tid];
-  if (ROUGH != SS_ROUGH_NONE)
-    for (int m = tid; m <= a.n_terms; m += blockDim.x)
-      lg[m] = (float)lgamma((double)m + 1.0);
+  if (ROUGH != SS_ROUGH_NONE) fill_inv_table(lg, a.n_terms, tid, blockDim.x);
   __syncthreads();
   if (tid == 0) {
     int lo = s_lo[0], hi = s_hi[0];

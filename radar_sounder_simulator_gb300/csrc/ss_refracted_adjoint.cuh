@@ -63,9 +63,7 @@ __device__ __forceinline__ void adjoint_stage_tables(const RefArgs &a,
     s_pat[pa_len + m] = (float)a.pb[m];
   if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
     s_fad[tid] = (float)a.fad.a[tid];
-  if (ROUGH != SS_ROUGH_NONE)
-    for (int m = tid; m <= a.n_terms; m += blockDim.x)
-      lg[m] = (float)lgamma((double)m + 1.0);
+  if (ROUGH != SS_ROUGH_NONE) fill_inv_table(lg, a.n_terms, tid, blockDim.x);
 }
 
 template <int NI, int ROUGH>

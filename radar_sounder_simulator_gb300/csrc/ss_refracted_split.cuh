@@ -1112,9 +1112,7 @@ __device__ __forceinline__ void refracted_split_cta(const RefArgs &a,
     s_fad[tid] = (float)a.fad.a[tid];
   for (int j = tid; j < a.tb * a.n_seg; j += blockDim.x)
     hist[j] = make_float2(0.0f, 0.0f);
-  if (ROUGH != SS_ROUGH_NONE)
-    for (int m = tid; m <= a.n_terms; m += blockDim.x)
-      lg[m] = (float)lgamma((double)m + 1.0);
+  if (ROUGH != SS_ROUGH_NONE) fill_inv_table(lg, a.n_terms, tid, blockDim.x);
   __syncthreads();
   if (tid == 0) {
     int lo = s_lo[0], hi = s_hi[0];
@@ -1240,9 +1238,7 @@ refracted_split_fixup(RefArgs a, RefSplitConsts k) {
     s_pat[pa_len + j] = (float)a.pb[j];
   if (ROUGH == SS_ROUGH_GAUSS_FULL && tid < SS_FAD_N)
     s_fad[tid] = (float)a.fad.a[tid];
-  if (ROUGH != SS_ROUGH_NONE)
-    for (int m = tid; m <= a.n_terms; m += blockDim.x)
-      lg[m] = (float)lgamma((double)m + 1.0);
+  if (ROUGH != SS_ROUGH_NONE) fill_inv_table(lg, a.n_terms, tid, blockDim.x);
   __syncthreads();
   const unsigned long long n_words =
       ((unsigned long long)a.T * a.defer_w + 31) >> 5;
@@ -1400,8 +1396,8 @@ template <int NI, int ROUGH>
 __global__ void __launch_bounds__(32 * kFixWarps, 4)
 refracted_batch_fixup(const RefBatchJob *jobs, int n_jobs,
                       long long n_words) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  float *lg = reinterpret_cast<float *>(smem_raw);
+  // the jobs' series lengths differ: no 1/m table (the series divides)
+  const float *lg = nullptr;
   __shared__ float s_pat[SS_PAT_MAX];
   __shared__ float s_fad[SS_FAD_N];
   __shared__ unsigned long long s_q[kFixWarps][kFixQueue];
