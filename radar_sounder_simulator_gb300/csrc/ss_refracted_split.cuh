@@ -98,14 +98,11 @@ __device__ __forceinline__ float dot3a(const float *a, const float *b) {
 __device__ __forceinline__ float sigma32(float ar, float bd, float Lh,
                                          float ah, float bh, float ratio,
                                          int n_iter, float sig0 = -1.0f) {
-  // start: the given sigma, else the paraxial root ar s + bd (ratio s) =
-  // Lh (Snell's law with tan ~ sin), much closer than the straight line
-  // for the strongly refracting air/ice crossing; the bracketed Newton
-  // below reaches the same root from either
   const float hi0 = 1.0f - 8.0f * kEps32;
   float sig = sig0 >= 0.0f
                   ? fminf(sig0, hi0)
-                  : fminf(Lh / fmaxf(ar + bd * ratio, kTiny32), hi0);
+                  : fminf(Lh / fmaxf(sqrtf(Lh * Lh + (ah + bh) * (ah + bh)),
+                                     kTiny32), hi0);
   float lo = 0.0f, hi = hi0;
   for (int it = 0; it < n_iter; ++it) {
     const float v = ratio * sig;
