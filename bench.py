@@ -61,7 +61,7 @@ def parse():
                          "(comma list, or 'none')")
     ap.add_argument("--batch-instances", type=int, default=96)
     ap.add_argument("--kernel-only", default=None,
-                    choices=["surface", "h1", "h2", "bed"],
+                    choices=["surface", "h1", "h2", "bed", "rough450"],
                     help="run only this target of the multilayer scene "
                          "(warm-up + steps launches, for profiling) and "
                          "print its mean time")
@@ -468,11 +468,32 @@ def main():
         dist.destroy_process_group()
 
 
+def rough_bed_450_plan(device):
+    """The roughness configuration's slowest job: the rough bed under the
+    surface (sequential refraction, area-only exponential series, taper) in
+    the 450 MHz band, all 2048 traces."""
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.multilayer import prepare_refracted
+    cfg = scenes.config3()
+    bd = scenes.config3_band(cfg, 450e6)
+    rb = cfg.rough["bed"]
+    return prepare_refracted(
+        cfg.pos, cfg.uct, cfg.bed, [cfg.surface], cfg.eps, cfg.att,
+        mode="coherent", t0=bd["t0"], dt=bd["dt"], n_samples=bd["n_s"],
+        c=cfg.c, gamma=cfg.gamma_bed, k0=bd["k0"],
+        roughness=(rb["sigma"], rb["corr"], rb["phasors"], bd["nt_b"],
+                   "exponential"), d_phi_area=True, taper_s=0.05,
+        refraction="sequential", precision="split", device=device)
+
+
 def run_kernel_only(args, plans, device):
     """One target's plan alone (main pass, fix-up, reduce): warm-up and
     timed launches, mean event time printed (the profiling entry point)."""
     import torch
-    p = plans[["surface", "h1", "h2", "bed"].index(args.kernel_only)]
+    if args.kernel_only == "rough450":
+        p = rough_bed_450_plan(device)
+    else:
+        p = plans[["surface", "h1", "h2", "bed"].index(args.kernel_only)]
     for _ in range(args.warmup):
         p.run()
     torch.cuda.synchronize()
