@@ -66,8 +66,12 @@ __device__ __forceinline__ void adjoint_stage_tables(const RefArgs &a,
   if (ROUGH != SS_ROUGH_NONE) fill_inv_table(lg, a.n_terms, tid, blockDim.x);
 }
 
+// The sequential chain fits 80 registers without spills: six 128-thread
+// CTAs per SM (24 warps) hide this latency-bound kernel's dependent chains
+// better than the 152 registers the compiler takes unasked. The joint
+// solves keep their registers (they spill heavily at 80).
 template <int NI, int ROUGH>
-__global__ void __launch_bounds__(kAdjThreads)
+__global__ void __launch_bounds__(kAdjThreads, NI == 0 ? 6 : 1)
 refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float *lg = reinterpret_cast<float *>(smem_raw);
