@@ -125,6 +125,7 @@ __device__ __forceinline__ float sigma32(float ar, float bd, float Lh,
 // Two-point solve with both end points relative to the plane point.
 struct Solve32 {
   float y[3];    // crossing relative to the plane point
+  float sig;     // the root sigma = sin(theta) on the rare side
   float c1, c2;  // cos(theta) on the p side and on the q side
   float res;     // Snell residual (closure form, like refraction.py:155)
   bool sides;    // end points strictly on opposite sides of the plane
@@ -166,6 +167,7 @@ __device__ __forceinline__ void snell_rel32(const float *P, const float *Q,
     sig0 = tr0 * rsqrtf(fmaxf(ar * ar + tr0 * tr0, kTiny32));
   }
   const float sig = sigma32(ar, bd, Lh, ah, bh, ratio, n_iter, sig0);
+  S.sig = sig;
   const float v = ratio * sig;
   const float tr = ar * sig * rsqrtf(fmaxf((1.0f - sig) * (1.0f + sig),
                                            kTiny32));
@@ -256,7 +258,7 @@ static __device__ __noinline__ void cell64(const ss_interface &I, const double *
 static __device__ __noinline__ bool snell_df(const df *p, const df *q,
                                          const df *o, const df *nrm,
                                          double n1, double n2, int n_iter,
-                                         df *x) {
+                                         df *x, float sig0) {
   const df tiny = df_make(1e-30f, 0.0f);
   df po[3], qo[3];
   for (int j = 0; j < 3; ++j) {
@@ -282,10 +284,14 @@ static __device__ __noinline__ bool snell_df(const df *p, const df *q,
   const df one = df_make(1.0f, 0.0f);
   const df hi0 = df_from_double(1.0 - 8.0 * kEps64);
   const df abh = df_add(ah, bh);
-  df sig = df_min(df_div(Lh, df_max(df_sqrt(df_add(df_mul(Lh, Lh),
-                                                   df_mul(abh, abh))),
-                                    tiny)),
-                  hi0);
+  // start: the float32 pass's root when given (within ~1e-7 of this one:
+  // two or three steps), else the float64 chain's straight-line start
+  df sig = sig0 >= 0.0f
+               ? df_min(df_make(sig0, 0.0f), hi0)
+               : df_min(df_div(Lh, df_max(df_sqrt(df_add(df_mul(Lh, Lh),
+                                                         df_mul(abh, abh))),
+                                          tiny)),
+                        hi0);
   df lo = df_make(0.0f, 0.0f), hi = hi0;
   float step = 1.0f;
   for (int it = 0; it < n_iter; ++it) {
@@ -322,13 +328,14 @@ static __device__ __noinline__ bool snell_df(const df *p, const df *q,
 // the float64 chain (cell64) decides.
 __device__ __forceinline__ bool cell_df(const ss_interface &I, const df *cur,
                                         const df *q, double n1, double n2,
-                                        df *x_out, int &row, int &col) {
+                                        df *x_out, int &row, int &col,
+                                        float sig0 = -1.0f) {
   df o[3], nrm[3], x[3];
   for (int j = 0; j < 3; ++j) {
     o[j] = df_from_double(I.mean_point[j]);
     nrm[j] = df_from_double(I.mean_normal[j]);
   }
-  if (!snell_df(cur, q, o, nrm, n1, n2, 10, x)) return false;
+  if (!snell_df(cur, q, o, nrm, n1, n2, 10, x, sig0)) return false;
   int idx[2];
   for (int c = 0; c < 2; ++c) {
     const df rc = df_add(df_add(df_mul(x[0], df_from_double(I.coef[c])),
@@ -457,7 +464,8 @@ __device__ __forceinline__ void path_sequential_split(const RefArgs &a,
         if (i > 0) cdf[j] = df_add_f(cdf[j], y_prev[j]);  // exact sum
         qdf[j] = df_make(q[j], 0.0f);
       }
-      if (!cell_df(I, cdf, qdf, a.n_leg[i], a.n_leg[i + 1], xdf, row, col)) {
+      if (!cell_df(I, cdf, qdf, a.n_leg[i], a.n_leg[i + 1], xdf, row, col,
+                   Sm.sig)) {
         double cur64[3], q64[3] = {q[0], q[1], q[2]}, x1[3];
         for (int j = 0; j < 3; ++j)
           cur64[j] = i == 0 ? p64[j] : (double)o_prev[j] + (double)y_prev[j];
@@ -553,7 +561,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   // pass 1: mean-plane chain anchors the lookups; its crossings (relative
   // to each mean point) also seed the joint solve
   int rows[NI], cols[NI];
-  float Xm[NI][3];
+  float Xm[NI][3], Sg[NI];
   {
     float Pm[3] = {T.pm0[0], T.pm0[1], T.pm0[2]};
     bool safe = true;
@@ -566,6 +574,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
       snell_rel32(Pm, Qm, M.mn, nm[i], nm[i + 1], 10, S);
       safe = cell_of(M, a.ifc[i], S.y, rows[i], cols[i]) && safe;
       for (int j = 0; j < 3; ++j) Pm[j] = Xm[i][j] = S.y[j];
+      Sg[i] = S.sig;
     }
     if (!safe) {  // the reference's float64 chain for this pair
       if (!EXACT) {
@@ -583,7 +592,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
       bool dfok = true;
       for (int i = 0; i < ni && dfok; ++i)
         dfok = cell_df(a.ifc[i], cdf, qdf, a.n_leg[i], a.n_leg[i + 1], cdf,
-                       rows[i], cols[i]);
+                       rows[i], cols[i], Sg[i]);
       if (!dfok) {
         double c64[3] = {p64[0], p64[1], p64[2]};
         const double q64[3] = {q[0], q[1], q[2]};
