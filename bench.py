@@ -577,11 +577,23 @@ def cfg1_cpu_baseline(cfg, seconds):
                       f"{el:.1f} s"}
 
 
+def df_fft_flop(n_fft):
+    """FP32 FLOP of one row's double-float FFT convolution (FMA = 2): per
+    radix-4 butterfly 16 double-float additions (11) and 3 twiddle products
+    (two exact-product dot products of 25), per radix-2 butterfly 4
+    additions, per point one spectrum product (50); two transforms."""
+    lg = int(np.log2(n_fft))
+    per_fft = (lg // 2) * (n_fft // 4) * (16 * 11 + 3 * 50) + \
+        (lg % 2) * (n_fft // 2) * 44
+    return 2.0 * per_fft + 50.0 * n_fft
+
+
 def row_cfg1(device, flush, peaks, cpu_seconds=0.0):
-    """Plain surface, delta-binned coherent sum + LFM pulse compression."""
+    """Plain surface, delta-binned coherent sum + LFM pulse compression,
+    the pulse transformed once per precision (``RangeCompressor``)."""
     from radar_sounder_simulator_gb300 import scenes
     from radar_sounder_simulator_gb300.coherent import prepare_coherent
-    from radar_sounder_simulator_gb300.waveform import (compress_tensor,
+    from radar_sounder_simulator_gb300.waveform import (RangeCompressor,
                                                          compressed_pulse)
     cfg = scenes.config1()
     f = cfg.facets
@@ -590,18 +602,22 @@ def row_cfg1(device, flush, peaks, cpu_seconds=0.0):
           for p in ("split", "fp64")}
     pulse, m = compressed_pulse(cfg.bw, cfg.pulse_length, cfg.kw["dt"],
                                 "hann", "chirp")
+    B = cfg.kw["n_samples"]
+    rc = {p: RangeCompressor(pulse, m, B, precision=p, device=device)
+          for p in ("split", "fp64")}
     out = {}
 
     def step(prec):
         fld, _ = pl[prec].run()
-        out[prec] = compress_tensor(fld, pulse, m)
+        out[prec] = rc[prec].run(fld)
     ms = _events_ms(lambda: step("split"), 5, flush)
     ms64 = _events_ms(lambda: step("fp64"), 2, flush)
     ms_k = _events_ms(lambda: pl["split"].run(), 5, flush)
     fld, _ = pl["split"].run()
-    ms_rc = _events_ms(lambda: compress_tensor(fld, pulse, m), 5, flush)
+    ms_rc = _events_ms(lambda: rc["split"].run(fld), 5, flush)
+    ms_rc64 = _events_ms(lambda: rc["fp64"].run(fld), 3, flush)
     pairs = len(f.centers) * len(cfg.pos)
-    T, B = len(cfg.pos), cfg.kw["n_samples"]
+    T = len(cfg.pos)
     n_fft = 1 << int(np.ceil(np.log2(B + len(pulse) - 1)))
     fft_flop = 2 * 5.0 * n_fft * np.log2(n_fft) + 6.0 * n_fft
     return {"workload": "surface_128sq_100m_256tr_2048bins_chirp_20us",
@@ -612,11 +628,18 @@ def row_cfg1(device, flush, peaks, cpu_seconds=0.0):
                               "surface facet sum (main pass + reduce), 47 "
                               "FLOP per smooth isotropic pair"),
             "range_compression": {
-                "taps": len(pulse), "ms": ms_rc, "method": "fft",
+                "taps": len(pulse), "ms": ms_rc, "method": "fft, "
+                "double-float transforms, pulse planned once",
                 "samples_per_s": T * B / (ms_rc * 1e-3),
-                "roofline": _roof(T * fft_flop, ms_rc, peaks["fp64"], "fp64",
-                                  fft_flop, f"float64 FFT convolution per "
-                                  f"row: 2 x 5 N log2 N + 6 N, N = {n_fft}")},
+                "roofline": _roof(T * df_fft_flop(n_fft), ms_rc,
+                                  peaks["fp32"], "fp32", df_fft_flop(n_fft),
+                                  f"double-float FFT convolution per row, "
+                                  f"N = {n_fft} (FP32 FLOP, FMA = 2)"),
+                "fp64_ms": ms_rc64,
+                "fp64_roofline": _roof(T * fft_flop, ms_rc64, peaks["fp64"],
+                                       "fp64", fft_flop,
+                                       f"float64 FFT convolution per row: "
+                                       f"2 x 5 N log2 N + 6 N, N = {n_fft}")},
             "error_vs_fp64": _errors(out["split"], out["fp64"]),
             "cpu_baseline": _cpu_or_error(
                 lambda: cfg1_cpu_baseline(cfg, cpu_seconds), cpu_seconds)}
@@ -736,7 +759,7 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32, cpu_seconds=0.0):
     from radar_sounder_simulator_gb300 import scenes
     from radar_sounder_simulator_gb300.coherent import prepare_coherent
     from radar_sounder_simulator_gb300.multilayer import prepare_refracted
-    from radar_sounder_simulator_gb300.waveform import (compress_tensor,
+    from radar_sounder_simulator_gb300.waveform import (RangeCompressor,
                                                          compressed_pulse)
     cfg = scenes.config3()
     s, b = cfg.surface, cfg.bed
@@ -765,12 +788,13 @@ def row_cfg3(device, flush, peaks, cfg3_error_traces=32, cpu_seconds=0.0):
             return ps, pb
         ps, pb = plans(cfg.pos, cfg.uct)
         pulse, m = compressed_pulse(bw, 10e-6, dt, "hann", "chirp")
+        rc = RangeCompressor(pulse, m, n_s, precision="split", device=device)
 
         def step():
             f1, _ = ps.run()
             f2, _ = pb.run()
-            compress_tensor(f1, pulse, m)
-            compress_tensor(f2, pulse, m)
+            rc.run(f1)
+            rc.run(f2)
         ms = _events_ms(step, 2, flush)
         ms_k = _events_ms(lambda: (ps.run(), pb.run()), 2, flush)
         T = len(cfg.pos)

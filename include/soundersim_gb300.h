@@ -534,6 +534,26 @@ int ss_range_compress_fft(const ss_waveform_opts *opts, const double *taps,
                           const void *in, void *out, void *scratch,
                           size_t scratch_bytes, void *stream);
 
+/* The FFT convolution in two steps, so that a pulse used for many arrays
+ * is transformed once (apply_waveform, waveform.py:141-160, compresses
+ * every kernel output with the same pulse): ss_range_compress_plan writes
+ * the twiddles and the pulse spectrum into `plan`; ss_range_compress_apply
+ * convolves one (T, B, L) array with them. Both take the same n_samples,
+ * n_taps, center and power (n_traces, n_lanes and in_f64 may differ
+ * between applies). precision: SS_PREC_FP64 (float64 transforms, as
+ * ss_range_compress_fft) or SS_PREC_SPLIT (double-float transforms on the
+ * FP32 pipe, ~1e-14 of the row's magnitude from the float64 ones, below
+ * the float32 rounding of the output). Plan size 0: n_samples + n_taps - 1
+ * is above 8192 (use ss_range_compress). Stream operations only. */
+size_t ss_range_compress_plan_bytes(const ss_waveform_opts *opts,
+                                    int precision);
+int ss_range_compress_plan(const ss_waveform_opts *opts, int precision,
+                           const double *taps, void *plan, size_t plan_bytes,
+                           void *stream);
+int ss_range_compress_apply(const ss_waveform_opts *opts, int precision,
+                            const void *plan, size_t plan_bytes,
+                            const void *in, void *out, void *stream);
+
 /* Frequency-sampled synthesis (Mode F). */
 typedef struct {
   double f0;          /* band centre (Hz) */

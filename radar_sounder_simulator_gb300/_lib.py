@@ -217,6 +217,14 @@ SIGNATURES = {
     "ss_range_compress_fft": (C.c_int, [C.POINTER(WaveformOpts), C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_void_p,
                                         C.c_size_t, C.c_void_p]),
+    "ss_range_compress_plan_bytes": (C.c_size_t, [C.POINTER(WaveformOpts),
+                                                  C.c_int32]),
+    "ss_range_compress_plan": (C.c_int, [C.POINTER(WaveformOpts), C.c_int32,
+                                         C.c_void_p, C.c_void_p, C.c_size_t,
+                                         C.c_void_p]),
+    "ss_range_compress_apply": (C.c_int, [C.POINTER(WaveformOpts), C.c_int32,
+                                          C.c_void_p, C.c_size_t, C.c_void_p,
+                                          C.c_void_p, C.c_void_p]),
     "ss_multifreq_scratch_bytes": (C.c_size_t, [C.POINTER(MultifreqOpts),
                                                 C.c_int32, C.c_int32]),
     "ss_multifreq_response": (C.c_int, [C.POINTER(MultifreqOpts),

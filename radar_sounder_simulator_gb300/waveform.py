@@ -7,8 +7,9 @@ Same functions and argument meaning as the reference module:
   on the host -- the analytic raised-cosine windowed sinc or the explicit
   LFM matched filter decimated onto the dt lattice;
 * ``convolve_fast_time(arr, kernel, center)`` (waveform.py:126-138) is the
-  'same'-mode fast-time convolution, run by ``ss_range_compress_fft``
-  (float64 FFT, the reference's method) or, beyond 8192 points,
+  'same'-mode fast-time convolution, run by ``ss_range_compress_plan`` /
+  ``ss_range_compress_apply`` (FFT, the reference's method, in float64 or
+  in double-float on the FP32 pipe) or, beyond 8192 points,
   ``ss_range_compress`` (compensated direct sum);
 * ``apply_waveform(out, radar, mode)`` (waveform.py:141-160) applies the
   configured waveform: identity for ``kind="delta"``, complex convolution
@@ -16,7 +17,8 @@ Same functions and argument meaning as the reference module:
   only when ``incoherent_envelope`` is set.
 
 ``compress_tensor`` is the device-resident form for callers that keep the
-kernel output on the GPU.
+kernel output on the GPU; ``RangeCompressor`` transforms a pulse once for
+many arrays.
 """
 
 import ctypes as C
@@ -74,18 +76,9 @@ def _chirp_pulse(bandwidth, pulse_length, dt, window):
     return p, m
 
 
-def compress_tensor(x, kernel, center, *, power=False, out=None,
-                    method="auto"):
-    """Device form: 'same'-mode convolution of ``x`` along dim 1.
-
-    ``x``: CUDA tensor (T, B[, L]) -- complex64/complex128, or float
-    (T, B[, L], 2) re/im pairs; with ``power`` a real (T, B[, L]) float
-    tensor. ``kernel``: 1-D taps (host array or tensor), zero lag at
-    ``center``. Returns complex64 (T, B[, L]) (float32 when ``power``),
-    launched on the current stream. ``method``: "fft" (float64 FFT in shared
-    memory, the reference's method; B + len(kernel) - 1 <= 8192), "direct"
-    (compensated direct sum, any size) or "auto" (FFT when it fits).
-    """
+def _stage(x, power):
+    """(re/im-paired or real) contiguous float view of ``x`` and its
+    (T, B[, L]) shape."""
     if not x.is_cuda:
         raise ValueError("compress_tensor needs a CUDA tensor")
     xr = x
@@ -103,43 +96,129 @@ def compress_tensor(x, kernel, center, *, power=False, out=None,
         raise ValueError("input must be (T, B) or (T, B, L)")
     if xr.dtype not in (torch.float32, torch.float64):
         xr = xr.to(torch.float64)
-    xr = xr.contiguous()
-    T, B = int(shape[0]), int(shape[1])
-    L = int(shape[2]) if len(shape) == 3 else 1
+    return xr.contiguous(), tuple(shape)
+
+
+def _taps(kernel, power, device):
     k = np.asarray(kernel)
     if power:
-        taps = torch.as_tensor(np.ascontiguousarray(k.real, np.float64),
-                               device=x.device)
-    else:
-        kc = np.asarray(k, np.complex128)
-        taps = torch.as_tensor(
-            np.ascontiguousarray(np.stack([kc.real, kc.imag], -1)),
-            device=x.device)
-    if out is None:
-        out = torch.empty(tuple(shape) + (() if power else (2,)),
-                          dtype=torch.float32, device=x.device)
-    o = _lib.WaveformOpts(T, B, L, len(k), int(center), int(bool(power)),
-                          int(xr.dtype == torch.float64))
-    stream = torch.cuda.current_stream(x.device).cuda_stream
-    L_ = _lib.lib()
-    nfft = L_.ss_range_compress_fft_scratch_bytes(C.byref(o))
-    if method == "fft" and nfft == 0:
-        raise ValueError("B + len(kernel) - 1 above 8192: use the direct sum")
+        return torch.as_tensor(np.ascontiguousarray(k.real, np.float64),
+                               device=device)
+    kc = np.asarray(k, np.complex128)
+    return torch.as_tensor(
+        np.ascontiguousarray(np.stack([kc.real, kc.imag], -1)), device=device)
+
+
+class RangeCompressor:
+    """A compressed pulse prepared for repeated 'same'-mode fast-time
+    convolutions of (T, ``n_samples``[, L]) arrays on the GPU -- the FFT
+    method of ``convolve_fast_time`` (waveform.py:126-138) with its pulse
+    transformed once: the constructor writes the twiddles and the pulse
+    spectrum (``ss_range_compress_plan``), each ``run`` is one launch
+    (``ss_range_compress_apply``, one CTA per row).
+
+    ``precision``: "fp64" (float64 transforms, the reference's arithmetic)
+    or "split" (double-float transforms on the FP32 pipe: ~1e-14 of each
+    row's magnitude from the float64 ones, below the float32 rounding of
+    the complex64 result). ``n_samples + len(kernel) - 1`` must be at most
+    8192 (``compress_tensor(method="direct")`` takes any size).
+    """
+
+    def __init__(self, kernel, center, n_samples, *, power=False,
+                 precision="fp64", device=None):
+        if precision not in _lib.PREC:
+            raise ValueError(f"unknown precision {precision!r}")
+        self.n_taps = len(np.asarray(kernel))
+        self.center, self.n_samples = int(center), int(n_samples)
+        self.power, self.precision = bool(power), precision
+        self.device = _device(device)
+        self._prec = _lib.PREC[precision]
+        o = self._opts(1, 1, False)
+        L_ = _lib.lib()
+        nb = L_.ss_range_compress_plan_bytes(C.byref(o), self._prec)
+        if self.n_taps <= 0 or not 0 <= self.center < self.n_taps or \
+                self.n_samples <= 0:
+            raise ValueError("need n_samples > 0 and 0 <= center < "
+                             "len(kernel)")
+        if nb == 0:
+            raise ValueError("B + len(kernel) - 1 above 8192: use the "
+                             "direct sum")
+        self._taps = _taps(kernel, self.power, self.device)
+        self.plan = torch.empty(nb, dtype=torch.uint8, device=self.device)
+        stream = torch.cuda.current_stream(self.device).cuda_stream
+        _lib.check(L_.ss_range_compress_plan(
+            C.byref(o), self._prec, C.c_void_p(self._taps.data_ptr()),
+            C.c_void_p(self.plan.data_ptr()), nb, C.c_void_p(stream)),
+            "ss_range_compress_plan")
+
+    def _opts(self, T, L, in_f64):
+        return _lib.WaveformOpts(T, self.n_samples, L, self.n_taps,
+                                 self.center, int(self.power), int(in_f64))
+
+    def run(self, x, out=None):
+        """Convolve ``x`` (CUDA, (T, B[, L]); complex64/complex128 or float
+        re/im pairs, real with ``power``) on the current stream; returns
+        complex64 (float32 clipped at 0 with ``power``)."""
+        xr, shape = _stage(x, self.power)
+        T, B = shape[0], shape[1]
+        L = shape[2] if len(shape) == 3 else 1
+        if B != self.n_samples:
+            raise ValueError(f"{B} samples per trace, the plan has "
+                             f"{self.n_samples}")
+        if out is None:
+            out = torch.empty(shape + (() if self.power else (2,)),
+                              dtype=torch.float32, device=x.device)
+        o = self._opts(T, L, xr.dtype == torch.float64)
+        stream = torch.cuda.current_stream(x.device).cuda_stream
+        _lib.check(_lib.lib().ss_range_compress_apply(
+            C.byref(o), self._prec, C.c_void_p(self.plan.data_ptr()),
+            self.plan.numel(), C.c_void_p(xr.data_ptr()),
+            C.c_void_p(out.data_ptr()), C.c_void_p(stream)),
+            "ss_range_compress_apply")
+        return out if self.power else torch.view_as_complex(out)
+
+
+def compress_tensor(x, kernel, center, *, power=False, out=None,
+                    method="auto", precision="fp64"):
+    """Device form: 'same'-mode convolution of ``x`` along dim 1.
+
+    ``x``: CUDA tensor (T, B[, L]) -- complex64/complex128, or float
+    (T, B[, L], 2) re/im pairs; with ``power`` a real (T, B[, L]) float
+    tensor. ``kernel``: 1-D taps (host array or tensor), zero lag at
+    ``center``. Returns complex64 (T, B[, L]) (float32 when ``power``),
+    launched on the current stream. ``method``: "fft" (FFT in shared
+    memory, the reference's method, in ``precision`` "fp64" or "split" as
+    ``RangeCompressor``; B + len(kernel) - 1 <= 8192), "direct"
+    (compensated direct sum, any size) or "auto" (FFT when it fits). A
+    pulse applied to many arrays is cheaper through one ``RangeCompressor``.
+    """
     if method not in ("auto", "fft", "direct"):
         raise ValueError(f"unknown method {method!r}")
-    if method != "direct" and nfft > 0:
-        scratch = torch.empty(nfft, dtype=torch.uint8, device=x.device)
-        st = L_.ss_range_compress_fft(
-            C.byref(o), C.c_void_p(taps.data_ptr()),
-            C.c_void_p(xr.data_ptr()), C.c_void_p(out.data_ptr()),
-            C.c_void_p(scratch.data_ptr()), nfft, C.c_void_p(stream))
-        _lib.check(st, "ss_range_compress_fft")
-    else:
-        st = L_.ss_range_compress(C.byref(o), C.c_void_p(taps.data_ptr()),
-                                  C.c_void_p(xr.data_ptr()),
-                                  C.c_void_p(out.data_ptr()),
-                                  C.c_void_p(stream))
-        _lib.check(st, "ss_range_compress")
+    xr, shape = _stage(x, power)
+    T, B = shape[0], shape[1]
+    L = shape[2] if len(shape) == 3 else 1
+    n_taps = len(np.asarray(kernel))
+    o = _lib.WaveformOpts(T, B, L, n_taps, int(center), int(bool(power)),
+                          int(xr.dtype == torch.float64))
+    L_ = _lib.lib()
+    fits = L_.ss_range_compress_plan_bytes(C.byref(o), 0) > 0
+    if method == "fft" and not fits:
+        raise ValueError("B + len(kernel) - 1 above 8192: use the direct sum")
+    if method != "direct" and fits:
+        if not 0 <= int(center) < n_taps:
+            raise ValueError("need 0 <= center < len(kernel)")
+        rc = RangeCompressor(kernel, center, B, power=power,
+                             precision=precision, device=x.device)
+        return rc.run(xr, out=out)
+    taps = _taps(kernel, power, x.device)
+    if out is None:
+        out = torch.empty(shape + (() if power else (2,)),
+                          dtype=torch.float32, device=x.device)
+    stream = torch.cuda.current_stream(x.device).cuda_stream
+    st = L_.ss_range_compress(C.byref(o), C.c_void_p(taps.data_ptr()),
+                              C.c_void_p(xr.data_ptr()),
+                              C.c_void_p(out.data_ptr()), C.c_void_p(stream))
+    _lib.check(st, "ss_range_compress")
     return out if power else torch.view_as_complex(out)
 
 
@@ -149,29 +228,33 @@ def _device(device):
     return torch.device("cuda", torch.cuda.current_device())
 
 
-def convolve_fast_time(arr, kernel, center, *, device=None):
+def convolve_fast_time(arr, kernel, center, *, device=None,
+                       precision="fp64"):
     """'Same'-mode convolution along axis 1 with the kernel's zero lag at
     ``center`` (waveform.py:126-138). ``arr`` is (traces, n_samples, ...)
     complex or real; returns complex128 of the same shape (computed on the
     GPU from the float32-rounded input, as the reference convolves the
-    kernels' complex64 output)."""
+    kernels' complex64 output). ``precision`` of the FFT transforms: "fp64"
+    or "split" (``RangeCompressor``)."""
     a = np.asarray(arr)
     dev = _device(device)
     shape = a.shape
     x = a.reshape(shape[0], shape[1], -1)
     xt = torch.as_tensor(np.ascontiguousarray(
         np.stack([x.real, x.imag], -1).astype(np.float32)), device=dev)
-    y = compress_tensor(xt, kernel, center)
+    y = compress_tensor(xt, kernel, center, precision=precision)
     return y.cpu().numpy().astype(np.complex128).reshape(shape)
 
 
-def apply_waveform(out, radar, mode, *, device=None):
+def apply_waveform(out, radar, mode, *, device=None, precision="fp64"):
     """Apply ``radar.waveform`` to a kernel output (waveform.py:141-160).
 
     Coherent: complex convolution with the compressed pulse, complex64
     result. Incoherent: |p|^2 power-envelope convolution, clipped at zero,
     float32 -- only when ``incoherent_envelope`` is set, else ``out`` is
     returned unchanged. ``kind="delta"`` returns ``out`` unchanged.
+    ``precision`` of the FFT transforms: "fp64" or "split"
+    (``RangeCompressor``).
     """
     wf = radar.waveform
     if wf.kind == "delta":
@@ -186,9 +269,10 @@ def apply_waveform(out, radar, mode, *, device=None):
     if mode == "coherent":
         x = a.reshape(shape[0], shape[1], -1).astype(np.complex64)
         xt = torch.as_tensor(np.ascontiguousarray(x), device=dev)
-        y = compress_tensor(xt, p, m)
+        y = compress_tensor(xt, p, m, precision=precision)
         return y.cpu().numpy().reshape(shape)
     x = a.reshape(shape[0], shape[1], -1).astype(np.float32)
     xt = torch.as_tensor(np.ascontiguousarray(x), device=dev)
-    y = compress_tensor(xt, np.abs(p) ** 2, m, power=True)
+    y = compress_tensor(xt, np.abs(p) ** 2, m, power=True,
+                        precision=precision)
     return y.cpu().numpy().reshape(shape)

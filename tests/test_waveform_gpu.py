@@ -148,3 +148,89 @@ def test_long_rows_fall_back_to_the_direct_sum():
         wf.compress_tensor(xt, p, m, method="fft")
     y = wf.compress_tensor(xt, p, m).cpu().numpy()
     _check(y, owf.convolve_fast_time(x, p, m))
+
+
+def _rows(seed, T, B, lanes=None):
+    rng = np.random.default_rng(seed)
+    shape = (T, B) if lanes is None else (T, B, lanes)
+    x = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+    x[:, ::13] *= 1e3                       # strong targets, weak sidelobes
+    return x
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("B,pulse_us", [(2048, 20e-6), (500, 8e-6),
+                                        (700, 8e-6), (300, 2e-6),
+                                        (5000, 30e-6)])
+def test_split_fft_matches_the_float64_fft(B, pulse_us):
+    """The double-float transforms against the float64 ones on the same
+    float32-rounded rows: each complex64 output within one float32 rounding
+    of the float64 result (plus 1e-12 of the peak), and both within the
+    oracle bounds. Sizes give N = 4096 and 1024 (radix-4 stages only), 2048,
+    512 and 8192 (odd log2: with the radix-2 stage; 8192 is the largest
+    plan)."""
+    import torch
+    x = _rows(8, 6, B).astype(np.complex64)
+    p, m = owf.compressed_pulse(15e6, pulse_us, 1.0 / 30e6, "hann", "chirp")
+    xt = torch.as_tensor(x, device="cuda")
+    y64 = wf.compress_tensor(xt, p, m, method="fft",
+                             precision="fp64").cpu().numpy()
+    ys = wf.compress_tensor(xt, p, m, method="fft",
+                            precision="split").cpu().numpy()
+    peak = np.abs(y64).max()
+    assert np.all(np.abs(ys - y64) <= 2.0 ** -23 * np.abs(y64) + 1e-12 * peak)
+    ref = owf.convolve_fast_time(x, p, m)
+    _check(ys, ref)
+    _check(y64, ref)
+
+
+@pytest.mark.gpu
+def test_split_fft_power_envelope_and_float64_input():
+    import torch
+    rng = np.random.default_rng(9)
+    pw = rng.exponential(size=(4, 1500))
+    pw[:, ::17] *= 1e4
+    p, m = owf.compressed_pulse(15e6, 10e-6, 1.0 / 30e6, "hann")
+    taps = np.abs(p) ** 2
+    # float64 input is rounded to float32 first, as the reference convolves
+    # the kernels' float32 output
+    y = wf.compress_tensor(torch.as_tensor(pw, device="cuda"), taps, m,
+                           power=True, precision="split").cpu().numpy()
+    ref = np.maximum(owf.convolve_fast_time(pw.astype(np.float32), taps,
+                                            m).real, 0.0)
+    assert y.dtype == np.float32 and (y >= 0).all()
+    assert np.abs(y - ref).max() <= 3e-7 * np.abs(ref).max()
+    xc = _rows(10, 3, 1500, lanes=2)        # complex128, split sides
+    yc = wf.compress_tensor(torch.as_tensor(xc, device="cuda"), p, m,
+                            precision="split").cpu().numpy()
+    for lane in range(2):
+        _check(yc[..., lane], owf.convolve_fast_time(
+            xc[..., lane].astype(np.complex64), p, m))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_range_compressor_reuses_one_plan(precision):
+    """One plan applied to arrays of different trace and lane counts gives
+    the one-call results bit for bit; a row length other than the plan's
+    is refused."""
+    import torch
+    p, m = owf.compressed_pulse(15e6, 8e-6, 1.0 / 30e6, "hann", "chirp")
+    rc = wf.RangeCompressor(p, m, 900, precision=precision, device="cuda")
+    for seed, lanes in ((11, None), (12, 2)):
+        xt = torch.as_tensor(_rows(seed, 5, 900, lanes).astype(np.complex64),
+                             device="cuda")
+        a = rc.run(xt).cpu().numpy()
+        b = wf.compress_tensor(xt, p, m, precision=precision).cpu().numpy()
+        np.testing.assert_array_equal(a, b)
+    with pytest.raises(ValueError):
+        rc.run(torch.zeros((2, 901), dtype=torch.complex64, device="cuda"))
+    with pytest.raises(ValueError):
+        wf.RangeCompressor(p, m, 8000, precision=precision, device="cuda")
+
+
+@pytest.mark.gpu
+def test_split_single_tap_is_identity():
+    x = np.random.default_rng(5).normal(size=(2, 300)).astype(np.complex64)
+    y = wf.convolve_fast_time(x, np.array([1.0]), 0, precision="split")
+    assert np.abs(y - x).max() <= 1e-12 * np.abs(x).max()
