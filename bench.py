@@ -61,9 +61,12 @@ def parse():
                          "(comma list, or 'none')")
     ap.add_argument("--batch-instances", type=int, default=96)
     ap.add_argument("--kernel-only", default=None,
-                    choices=["surface", "h1", "h2", "bed", "rough450"],
-                    help="run only this target of the multilayer scene "
-                         "(warm-up + steps launches, for profiling) and "
+                    choices=["surface", "h1", "h2", "bed", "rough450",
+                             "plain128", "compress"],
+                    help="run only this target -- a multilayer-scene "
+                         "target, the rough bed at 450 MHz, the plain 128^2 "
+                         "surface's facet sum or its pulse compression "
+                         "(warm-up + steps launches, for profiling) -- and "
                          "print its mean time")
     ap.add_argument("--fp64-traces", type=int, default=256,
                     help="traces of the float64-form step (its rate is per "
@@ -486,12 +489,38 @@ def rough_bed_450_plan(device):
         refraction="sequential", precision="split", device=device)
 
 
+def plain_surface_plan(device, compress):
+    """The plain 128^2 surface's split facet sum over 256 traces, or (with
+    ``compress``) the double-float FFT compression of its field with the
+    20 us chirp (1201 taps, N = 4096), as a plan-like object."""
+    from types import SimpleNamespace
+    from radar_sounder_simulator_gb300 import scenes
+    from radar_sounder_simulator_gb300.coherent import prepare_coherent
+    from radar_sounder_simulator_gb300.waveform import (RangeCompressor,
+                                                         compressed_pulse)
+    cfg = scenes.config1()
+    f = cfg.facets
+    pl = prepare_coherent(cfg.pos, cfg.uct, f.centers, f.normals, f.areas,
+                          f.e1, f.e2, **cfg.kw, precision="split",
+                          device=device)
+    if not compress:
+        return pl
+    pulse, m = compressed_pulse(cfg.bw, cfg.pulse_length, cfg.kw["dt"],
+                                "hann", "chirp")
+    rc = RangeCompressor(pulse, m, cfg.kw["n_samples"], precision="split",
+                         device=device)
+    fld, _ = pl.run()
+    return SimpleNamespace(run=lambda: rc.run(fld))
+
+
 def run_kernel_only(args, plans, device):
     """One target's plan alone (main pass, fix-up, reduce): warm-up and
     timed launches, mean event time printed (the profiling entry point)."""
     import torch
     if args.kernel_only == "rough450":
         p = rough_bed_450_plan(device)
+    elif args.kernel_only in ("plain128", "compress"):
+        p = plain_surface_plan(device, args.kernel_only == "compress")
     else:
         p = plans[["surface", "h1", "h2", "bed"].index(args.kernel_only)]
     for _ in range(args.warmup):

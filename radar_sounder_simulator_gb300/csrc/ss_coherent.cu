@@ -266,11 +266,13 @@ int coherent_plan(const ss_coherent_opts *o, int T, int N, Plan *p,
   const int max_chunks = (int)std::max<long>(1, window / 512);
   // resident CTAs per SM: 2 (512-thread smooth split, 96 KB FP64), 3
   // (rough split at 80 registers); the chunk count whose item total fills
-  // 2-4 whole waves best (a last wave a tenth full costs a full wave)
+  // 1-4 whole waves best (a last wave a tenth full costs a full wave); on
+  // a tie the fewest waves, whose CTAs zero, fill and write their
+  // histograms fewer times per pair
   const long slots = (long)sm_count() * (fp64 ? 2 : (rough ? 3 : 2));
   int best = 1;
   double best_eff = -1.0;
-  for (int k = 2; k <= 4; ++k) {
+  for (int k = 1; k <= 4; ++k) {
     const int nc = (int)std::max<long>(
         1, std::min<long>(max_chunks, k * slots / p->n_groups));
     const long items = (long)nc * p->n_groups;

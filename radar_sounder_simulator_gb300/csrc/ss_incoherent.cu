@@ -26,6 +26,7 @@
 // second kernel sums the chunks in a fixed order in float64.
 #include <algorithm>
 
+#include "ss_chunksum.cuh"
 #include "ss_f32.cuh"
 #include "ss_internal.cuh"
 
@@ -185,7 +186,8 @@ incoherent_kernel(IncArgs a) {
     a.part_drop[(size_t)blockIdx.x * a.T + t_base + tid] = (double)s_drop[tid];
 }
 
-// Chunk sums in float64, in chunk order, into the (T, n[, 2]) float32 layout.
+// Chunk sums (compensated float32, ~2^-48 relative), in chunk order, into
+// the (T, n[, 2]) float32 layout.
 __global__ void incoherent_reduce_kernel(const float *part,
                                          const double *part_drop, int T,
                                          int n_seg, int n_samples, int split,
@@ -196,9 +198,10 @@ __global__ void incoherent_reduce_kernel(const float *part,
        e += (long)gridDim.x * blockDim.x) {
     const int t = (int)(e / n_seg);
     const int b = (int)(e % n_seg);
-    double s = 0.0;
+    ChunkSum<float> cs;
     for (int c = 0; c < n_chunks; ++c)
-      s += (double)part[((size_t)c * T + t) * n_seg + b];
+      cs.add(part[((size_t)c * T + t) * n_seg + b]);
+    const double s = cs.value();
     long o = e;
     if (split) {  // (T, 2, n) -> (T, n, 2) [left, right]
       const int side = b / n_samples, bl = b % n_samples;

@@ -1,39 +1,41 @@
 // Ordered reduction of per-CTA partial histograms into the output layout.
+#include <algorithm>
+
+#include "ss_chunksum.cuh"
 #include "ss_coherent.cuh"
 
 namespace ss {
 
+// grid: x over segments of a trace, y over traces (one element a thread,
+// the chunk loads of an element independent of one another)
 template <typename P>
 __global__ void chunk_reduce_kernel(ReduceArgs r, ss_output out) {
   const P *part = reinterpret_cast<const P *>(r.part);
-  const long total = (long)r.T * r.n_seg;
-  for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
-       e += (long)gridDim.x * blockDim.x) {
-    const int t = (int)(e / r.n_seg);
-    const int b = (int)(e % r.n_seg);
-    double sr = 0.0, si = 0.0;
-    for (int c = 0; c < r.n_chunks; ++c) {
-      const P v = part[((size_t)c * r.T + t) * r.n_seg + b];
-      sr += (double)v.x;
-      si += (double)v.y;
-    }
-    long o = e;
-    if (r.split) {  // (T, 2, n) -> (T, n, 2) [left, right]
-      const int side = b / r.n_samples, bl = b % r.n_samples;
-      o = ((long)t * r.n_samples + bl) * 2 + side;
-    }
-    if (out.field_c128) {
-      out.field_c128[2 * o] = sr;
-      out.field_c128[2 * o + 1] = si;
-    } else {
-      out.field_c64[2 * o] = (float)sr;
-      out.field_c64[2 * o + 1] = (float)si;
-    }
-    if (b == 0) {
-      double d = 0.0;
+  for (int t = blockIdx.y; t < r.T; t += gridDim.y) {
+    for (int b = blockIdx.x * blockDim.x + threadIdx.x; b < r.n_seg;
+         b += gridDim.x * blockDim.x) {
+      ChunkSum<P> s;
       for (int c = 0; c < r.n_chunks; ++c)
-        d += r.part_drop[(size_t)c * r.T + t];
-      out.dropped[t] = d;
+        s.add(part[((size_t)c * r.T + t) * r.n_seg + b]);
+      long o = (long)t * r.n_seg + b;
+      if (r.split) {  // (T, 2, n) -> (T, n, 2) [left, right]
+        const int side = b / r.n_samples, bl = b % r.n_samples;
+        o = ((long)t * r.n_samples + bl) * 2 + side;
+      }
+      const double sr = s.re(), si = s.im();
+      if (out.field_c128) {
+        out.field_c128[2 * o] = sr;
+        out.field_c128[2 * o + 1] = si;
+      } else {
+        out.field_c64[2 * o] = (float)sr;
+        out.field_c64[2 * o + 1] = (float)si;
+      }
+      if (b == 0) {
+        double d = 0.0;
+        for (int c = 0; c < r.n_chunks; ++c)
+          d += r.part_drop[(size_t)c * r.T + t];
+        out.dropped[t] = d;
+      }
     }
   }
 }
@@ -51,12 +53,10 @@ __global__ void batch_reduce_kernel(const BatchJob *jobs, int n_jobs,
     const int t = (int)(local / a.n_seg);
     const int b = (int)(local % a.n_seg);
     const P *part = reinterpret_cast<const P *>(a.part);
-    double sr = 0.0, si = 0.0;
-    for (int c = 0; c < J.n_chunks; ++c) {
-      const P v = part[((size_t)c * a.T + t) * a.n_seg + b];
-      sr += (double)v.x;
-      si += (double)v.y;
-    }
+    ChunkSum<P> s;
+    for (int c = 0; c < J.n_chunks; ++c)
+      s.add(part[((size_t)c * a.T + t) * a.n_seg + b]);
+    const double sr = s.re(), si = s.im();
     long o = (long)local;
     if (a.split) {
       const int side = b / a.n_samples, bl = b % a.n_samples;
@@ -101,7 +101,8 @@ int sm_count() {
 
 int launch_reduce(const ReduceArgs &r, bool f64_parts, const ss_output *out,
                   cudaStream_t st) {
-  const int grid = 4 * sm_count();
+  const dim3 grid((unsigned)std::min((r.n_seg + 255) / 256, 65535),
+                  (unsigned)std::min(r.T, 65535));
   if (f64_parts)
     chunk_reduce_kernel<double2><<<grid, 256, 0, st>>>(r, *out);
   else

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <vector>
 
+#include "ss_chunksum.cuh"
 #include "ss_refracted_split.cuh"
 
 namespace ss {
@@ -38,12 +39,10 @@ __global__ void refracted_batch_reduce(const RefBatchJob *jobs, int n_jobs,
     const int t = (int)(local / a.n_seg);
     const int b = (int)(local % a.n_seg);
     const float2 *part = reinterpret_cast<const float2 *>(a.part);
-    double sr = 0.0, si = 0.0;
-    for (int c = 0; c < J.n_chunks; ++c) {
-      const float2 v = part[((size_t)c * a.T + t) * a.n_seg + b];
-      sr += (double)v.x;
-      si += (double)v.y;
-    }
+    ChunkSum<float2> s;
+    for (int c = 0; c < J.n_chunks; ++c)
+      s.add(part[((size_t)c * a.T + t) * a.n_seg + b]);
+    const double sr = s.re(), si = s.im();
     long o = (long)local;
     if (a.split) {  // (T, 2, n) -> (T, n, 2) [left, right]
       const int side = b / a.n_samples, bl = b % a.n_samples;
