@@ -564,7 +564,7 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
   float Xm[NI][3], Sg[NI];
   {
     float Pm[3] = {T.pm0[0], T.pm0[1], T.pm0[2]};
-    bool safe = true;
+    int last_unsafe = -1;
     for (int i = 0; i < ni; ++i) {
       const MeanPlane32 &M = k.mean[i];
       if (i > 0)
@@ -572,25 +572,27 @@ __device__ __forceinline__ void path_joint_split(const RefArgs &a, const RefSpli
       const float Qm[3] = {q[0] - M.mp[0], q[1] - M.mp[1], q[2] - M.mp[2]};
       Solve32 S;
       snell_rel32(Pm, Qm, M.mn, nm[i], nm[i + 1], 10, S);
-      safe = cell_of(M, a.ifc[i], S.y, rows[i], cols[i]) && safe;
+      if (!cell_of(M, a.ifc[i], S.y, rows[i], cols[i])) last_unsafe = i;
       for (int j = 0; j < 3; ++j) Pm[j] = Xm[i][j] = S.y[j];
       Sg[i] = S.sig;
     }
-    if (!safe) {  // the reference's float64 chain for this pair
+    if (last_unsafe >= 0) {  // the reference's float64 chain for this pair
       if (!EXACT) {
         P.defer = true;
         return;
       }
-      // the double-float chain decides every cell unless a crossing is
-      // within 1e-8 cells of a boundary; then the float64 chain of the
-      // reference decides them all
+      // the double-float chain decides the cells up to the last one the
+      // float32 chain left undecided (the mean-plane chain does not depend
+      // on the cells, so the later float32 decisions stand) unless a
+      // crossing is within 1e-8 cells of a boundary; then the float64
+      // chain of the reference decides them all
       df cdf[3], qdf[3];
       for (int j = 0; j < 3; ++j) {
         cdf[j] = df_from_double(p64[j]);
         qdf[j] = df_make(q[j], 0.0f);
       }
       bool dfok = true;
-      for (int i = 0; i < ni && dfok; ++i)
+      for (int i = 0; i <= last_unsafe && dfok; ++i)
         dfok = cell_df(a.ifc[i], cdf, qdf, a.n_leg[i], a.n_leg[i + 1], cdf,
                        rows[i], cols[i], Sg[i]);
       if (!dfok) {
