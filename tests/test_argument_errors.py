@@ -120,3 +120,44 @@ def test_incoherent_and_multifreq_argument_errors():
     with pytest.raises(ValueError, match="per-facet gamma shape"):
         multifreq_traces(POS, BED.centers, BED.normals, BED.areas, BED.e1,
                          BED.e2, gamma=np.zeros(N + 2), **common)
+
+
+def test_range_compression_plan_and_apply_check_arguments_first():
+    """The pulse-compression plan and apply entry points refuse bad sizes,
+    precisions, null pointers and short plan buffers with their status
+    codes before any device work (a call that reached a kernel launch on
+    this host would return SS_ERR_CUDA instead)."""
+    import ctypes as C
+    from radar_sounder_simulator_gb300 import _lib
+    L = _lib.lib()
+    split, fp64 = _lib.PREC["split"], _lib.PREC["fp64"]
+    ok = _lib.WaveformOpts(4, 2048, 1, 1201, 600, 0, 0)
+    # plan sizes: 32 N bytes (double-float), 24 N bytes (float64), N = 4096
+    assert L.ss_range_compress_plan_bytes(C.byref(ok), split) == 32 * 4096
+    assert L.ss_range_compress_plan_bytes(C.byref(ok), fp64) == 24 * 4096
+    assert L.ss_range_compress_plan_bytes(C.byref(ok), 7) == 0
+    big = _lib.WaveformOpts(4, 8000, 1, 1201, 600, 0, 0)
+    assert L.ss_range_compress_plan_bytes(C.byref(big), split) == 0
+    dummy = C.c_void_p(256)   # never dereferenced: every call below fails
+    nb = 32 * 4096
+    bad_center = _lib.WaveformOpts(4, 2048, 1, 1201, 1201, 0, 0)
+    cases = [
+        (L.ss_range_compress_plan(C.byref(ok), split, None, dummy, nb, None),
+         _lib.SS_ERR_ARG),
+        (L.ss_range_compress_plan(C.byref(bad_center), split, dummy, dummy,
+                                  nb, None), _lib.SS_ERR_ARG),
+        (L.ss_range_compress_plan(C.byref(ok), 7, dummy, dummy, nb, None),
+         _lib.SS_ERR_ARG),
+        (L.ss_range_compress_plan(C.byref(big), split, dummy, dummy, nb,
+                                  None), _lib.SS_ERR_UNSUPPORTED),
+        (L.ss_range_compress_plan(C.byref(ok), split, dummy, dummy, nb - 16,
+                                  None), _lib.SS_ERR_SCRATCH),
+        (L.ss_range_compress_apply(C.byref(ok), split, dummy, nb, None, dummy,
+                                   None), _lib.SS_ERR_ARG),
+        (L.ss_range_compress_apply(C.byref(ok), fp64, dummy, 24 * 4096 - 1,
+                                   dummy, dummy, None), _lib.SS_ERR_SCRATCH),
+        (L.ss_range_compress_apply(C.byref(bad_center), split, dummy, nb,
+                                   dummy, dummy, None), _lib.SS_ERR_ARG),
+    ]
+    for got, want in cases:
+        assert got == want
