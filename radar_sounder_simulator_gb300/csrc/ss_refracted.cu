@@ -202,9 +202,33 @@ static int refracted_plan(const ss_refracted_opts *o, int T, int N, Plan *p) {
   p->threads = o->precision == SS_PREC_FP64 ? 128 : kSplitThreads;
   const long window = std::min<long>((long)o->n_win * o->block_size, N);
   const int max_chunks = (int)std::max<long>(1, window / 256);
-  const int target = 8 * sm_count();
-  p->n_chunks = std::max(1, std::min(max_chunks,
-                                     (target + p->n_groups - 1) / p->n_groups));
+  if (o->precision == SS_PREC_FP64) {
+    const int target = 8 * sm_count();
+    p->n_chunks = std::max(
+        1, std::min(max_chunks, (target + p->n_groups - 1) / p->n_groups));
+  } else {
+    // resident CTAs per SM of the split kernel that runs: two 512-thread
+    // CTAs (64 registers) for the sequential chain and joint solves through
+    // up to two interfaces, one (~128 registers) through three or more; the
+    // chunk count whose item total fills 4-12 whole waves best (a last
+    // wave half full costs a full one), the fewest waves on a tie
+    const long slots = (long)sm_count() *
+                       (!o->joint || o->n_crossed <= 2 ? 2 : 1);
+    int best = 1;
+    double best_eff = -1.0;
+    for (int k = 4; k <= 12; ++k) {
+      const int nc = (int)std::max<long>(
+          1, std::min<long>(max_chunks, k * slots / p->n_groups));
+      const long items = (long)nc * p->n_groups;
+      const long waves = (items + slots - 1) / slots;
+      const double eff = (double)items / (double)(waves * slots);
+      if (eff > best_eff + 1e-9) {
+        best_eff = eff;
+        best = nc;
+      }
+    }
+    p->n_chunks = best;
+  }
   p->smem = (size_t)tb * per_trace;
   return SS_OK;
 }
