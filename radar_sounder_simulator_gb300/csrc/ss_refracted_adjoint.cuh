@@ -70,6 +70,11 @@ __device__ __forceinline__ void adjoint_stage_tables(const RefArgs &a,
 // CTAs per SM (24 warps) hide this latency-bound kernel's dependent chains
 // better than the 152 registers the compiler takes unasked. The joint
 // solves keep their registers (they spill heavily at 80).
+//
+// Grid: x = facet blocks (thread <-> facet), y = parts of the trace range.
+// With one part a CTA writes its facets' sums and its alpha partial; with
+// several (chosen so the grid fills whole waves) each part adds them to
+// outputs the launch has zeroed.
 template <int NI, int ROUGH>
 __global__ void __launch_bounds__(kAdjThreads, NI == 0 ? 6 : 1)
 refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
@@ -95,9 +100,12 @@ refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
     q[1] = a.F.cy[i];
     q[2] = a.F.cz[i];
   }
+  const int parts = gridDim.y;
+  const int t_begin = (int)((long)a.T * blockIdx.y / parts);
+  const int t_end = (int)((long)a.T * (blockIdx.y + 1) / parts);
   double gR = 0.0, gS = 0.0, gA = 0.0;
-  for (int t0 = 0; t0 < a.T; t0 += kAdjTB) {
-    const int nt = min(kAdjTB, a.T - t0);
+  for (int t0 = t_begin; t0 < t_end; t0 += kAdjTB) {
+    const int nt = min(kAdjTB, t_end - t0);
     __syncthreads();
     if (tid < nt) {
       const int t = t0 + tid;
@@ -125,8 +133,13 @@ refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
   }
   // d c / d gamma_dB = c ln(10) / 20; d c / d alpha = -c ln(10) / 10 dloss
   if (i < a.N) {
-    j.grad_gamma_db[i] = gR * (kLn10 / 20.0);
-    if (j.grad_sigma) j.grad_sigma[i] = gS;
+    if (parts == 1) {
+      j.grad_gamma_db[i] = gR * (kLn10 / 20.0);
+      if (j.grad_sigma) j.grad_sigma[i] = gS;
+    } else {
+      atomicAdd(&j.grad_gamma_db[i], gR * (kLn10 / 20.0));
+      if (j.grad_sigma) atomicAdd(&j.grad_sigma[i], gS);
+    }
   }
   gA *= -kLn10 / 10.0;
   for (int d = 16; d > 0; d >>= 1) gA += __shfl_down_sync(0xffffffffu, gA, d);
@@ -135,7 +148,10 @@ refracted_adjoint_kernel(RefArgs a, RefSplitConsts k, AdjArgs j) {
   if (tid == 0) {
     double s = 0.0;
     for (int w = 0; w < kAdjThreads / 32; ++w) s += s_red[w];
-    j.grad_alpha[blockIdx.x] = s;
+    if (parts == 1)
+      j.grad_alpha[blockIdx.x] = s;
+    else
+      atomicAdd(&j.grad_alpha[blockIdx.x], s);
   }
 }
 
@@ -210,8 +226,42 @@ template <int NI, int ROUGH>
 inline int adjoint_launch_r(RefArgs &a, const RefSplitConsts &k,
                             const AdjArgs &j, size_t smem, cudaStream_t st) {
   const int blocks = refracted_adjoint_blocks(a.N);
-  refracted_adjoint_kernel<NI, ROUGH><<<blocks, kAdjThreads, smem, st>>>(a, k, j);
-  cudaError_t e = cudaGetLastError();
+  // trace parts: the count (up to 8) whose grid fills whole waves of the
+  // resident CTAs best, for grids under eight waves (a last wave a quarter
+  // full costs a full one); the fewest parts on a tie
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, refracted_adjoint_kernel<NI, ROUGH>, kAdjThreads, smem) !=
+          cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  const long slots = (long)per_sm * sm_count();
+  int parts = 1;
+  if ((long)blocks < 8 * slots) {
+    double best = -1.0;
+    for (int pp = 1; pp <= 8 && pp <= a.T; ++pp) {
+      const long items = (long)blocks * pp;
+      const long waves = (items + slots - 1) / slots;
+      const double eff = (double)items / (double)(waves * slots);
+      if (eff > best + 1e-9) {
+        best = eff;
+        parts = pp;
+      }
+    }
+  }
+  cudaError_t e;
+  if (parts > 1) {
+    e = cudaMemsetAsync(j.grad_gamma_db, 0, (size_t)a.N * sizeof(double), st);
+    if (e == cudaSuccess && j.grad_sigma)
+      e = cudaMemsetAsync(j.grad_sigma, 0, (size_t)a.N * sizeof(double), st);
+    if (e == cudaSuccess)
+      e = cudaMemsetAsync(j.grad_alpha, 0, (size_t)blocks * sizeof(double),
+                          st);
+    if (e != cudaSuccess) return cuda_status(e, "adjoint output clear");
+  }
+  refracted_adjoint_kernel<NI, ROUGH>
+      <<<dim3(blocks, parts), kAdjThreads, smem, st>>>(a, k, j);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "refracted adjoint launch");
   const unsigned long long n_words =
       ((unsigned long long)a.T * a.N + 31) >> 5;
