@@ -91,6 +91,25 @@ static int batch_layout(const ss_coherent_job *jobs, int n_jobs,
   // equal-work items: pairs per item ~ total / (items_per_sm x SMs)
   const double per_item =
       std::max(1.0, total_pairs / ((double)ips * sm_count()));
+  // the costliest jobs' items first (longest-processing-time order): a
+  // pair's cost grows with the job's series length, and a queue that ends
+  // on the cheapest items leaves the persistent grid a short tail; each
+  // job keeps its own outputs, so the table order is free
+  std::vector<int> order(n_jobs);
+  for (int j = 0; j < n_jobs; ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return L.jobs[x].a.n_terms > L.jobs[y].a.n_terms;
+  });
+  {
+    std::vector<BatchJob> sorted(n_jobs);
+    std::vector<long> win(n_jobs);
+    for (int r = 0; r < n_jobs; ++r) {
+      sorted[r] = L.jobs[order[r]];
+      win[r] = window[order[r]];
+    }
+    L.jobs.swap(sorted);
+    window.swap(win);
+  }
   size_t off = L.table_off + align256(sizeof(BatchJob) * n_jobs);
   long long item = 0, out = 0;
   for (int j = 0; j < n_jobs; ++j) {
@@ -106,7 +125,7 @@ static int batch_layout(const ss_coherent_job *jobs, int n_jobs,
     item += (long long)J.n_chunks * J.n_groups;
     out += (long long)a.T * a.n_seg;
     J.k = coherent_split_consts(a);
-    J.out = jobs[j].out;
+    J.out = jobs[order[j]].out;
     const size_t elt = a.precision == SS_PREC_FP64 ? 16 : 8;
     a.part = reinterpret_cast<void *>(off);  // offset until prepare
     off += align256((size_t)J.n_chunks * a.T * a.n_seg * elt);

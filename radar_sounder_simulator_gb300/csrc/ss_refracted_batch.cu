@@ -141,6 +141,26 @@ static int ref_batch_layout(const ss_refracted_job *jobs, int n_jobs,
   }
   const double per_item =
       std::max(1.0, total_pairs / ((double)ips * sm_count()));
+  // The queue serves the costliest jobs first (longest-processing-time
+  // order): items hold about equal pair counts, a pair's cost grows with
+  // the job's series length, and a queue that ends on the cheapest items
+  // leaves the persistent grid a short tail. Each job keeps its own
+  // outputs, so the table order is free.
+  std::vector<int> order(n_jobs);
+  for (int j = 0; j < n_jobs; ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+    return L.jobs[x].a.n_terms > L.jobs[y].a.n_terms;
+  });
+  {
+    std::vector<RefBatchJob> sorted(n_jobs);
+    std::vector<long long> win(n_jobs);
+    for (int r = 0; r < n_jobs; ++r) {
+      sorted[r] = L.jobs[order[r]];
+      win[r] = window[order[r]];
+    }
+    L.jobs.swap(sorted);
+    window.swap(win);
+  }
   size_t off = L.table_off + rb_align256(sizeof(RefBatchJob) * n_jobs);
   long long item = 0, out = 0, word = 0;
   for (int j = 0; j < n_jobs; ++j) {
@@ -160,7 +180,7 @@ static int ref_batch_layout(const ss_refracted_job *jobs, int n_jobs,
     J.words = (long long)(((unsigned long long)a.T * a.defer_w + 31) / 32);
     J.word0 = word;
     word += (J.words + 31) / 32 * 32;  // 32-word groups never straddle jobs
-    J.out = jobs[j].out;
+    J.out = jobs[order[j]].out;
     a.part = reinterpret_cast<void *>(off);  // offsets until prepare
     off += rb_align256((size_t)J.n_chunks * a.T * a.n_seg * sizeof(float2));
     a.part_drop = reinterpret_cast<double *>(off);
