@@ -77,9 +77,13 @@ static int batch_layout(const ss_coherent_job *jobs, int n_jobs,
       set_error("512-thread batches take smooth split-precision jobs only");
       return SS_ERR_ARG;
     }
+    // histogram budget as the one-call plan: rough split jobs (80
+    // registers, three 256-thread CTAs per SM) 48 KB, so three CTAs fit
     const size_t elt = a.precision == SS_PREC_FP64 ? 16 : 8;
-    const size_t budget = a.precision == SS_PREC_FP64 ? 96 * 1024
-                                                      : 100 * 1024;
+    const size_t budget =
+        a.precision == SS_PREC_FP64
+            ? 96 * 1024
+            : (a.rough_kind != SS_ROUGH_NONE ? 48 * 1024 : 100 * 1024);
     const size_t per_trace = (size_t)a.n_seg * elt;
     a.tb = (int)std::min<size_t>(
         std::max<size_t>(1, std::min<size_t>(budget / per_trace, max_tb)),
