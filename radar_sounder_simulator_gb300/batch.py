@@ -245,7 +245,7 @@ class RefractedBatch:
                                       dropped.data_ptr())
         self.jobs = jobs
         self.scratch = None
-        self.prepare(tuning or (512, 8, 8, 0))
+        self.prepare(tuning or (512, 8, 16, 0))
 
     def prepare(self, tuning):
         """Lay out scratch and upload the job table for ``tuning`` =
