@@ -91,7 +91,7 @@ static int ref_batch_layout(const ss_refracted_job *jobs, int n_jobs,
     set_error("batch max_tb must be in 1..8");
     return SS_ERR_ARG;
   }
-  const int ips = tune && tune->items_per_sm ? tune->items_per_sm : 8;
+  const int ips = tune && tune->items_per_sm ? tune->items_per_sm : 16;
   if (ips < 1) {
     set_error("batch items_per_sm must be positive");
     return SS_ERR_ARG;
