@@ -37,8 +37,8 @@
 //
 // Everything else (incidence, sincs, taper, antenna gain, roughness series)
 // runs in float32 from q + w and the facet's per-block products;
-// histograms accumulate float32 per CTA chunk and chunks are summed in
-// float64 by the reduce kernel.
+// histograms accumulate float32 per CTA chunk and the reduce kernel sums
+// the chunks by float32 two-sums (~2^-48 relative).
 #include <algorithm>
 
 #include "ss_coherent.cuh"
