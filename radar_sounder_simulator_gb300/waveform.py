@@ -131,18 +131,19 @@ class RangeCompressor:
         self.n_taps = len(np.asarray(kernel))
         self.center, self.n_samples = int(center), int(n_samples)
         self.power, self.precision = bool(power), precision
-        self.device = _device(device)
         self._prec = _lib.PREC[precision]
-        o = self._opts(1, 1, False)
-        L_ = _lib.lib()
-        nb = L_.ss_range_compress_plan_bytes(C.byref(o), self._prec)
         if self.n_taps <= 0 or not 0 <= self.center < self.n_taps or \
                 self.n_samples <= 0:
             raise ValueError("need n_samples > 0 and 0 <= center < "
                              "len(kernel)")
+        o = self._opts(1, 1, False)
+        L_ = _lib.lib()
+        nb = L_.ss_range_compress_plan_bytes(C.byref(o), self._prec)
         if nb == 0:
             raise ValueError("B + len(kernel) - 1 above 8192: use the "
                              "direct sum")
+        # arguments checked: only now the device
+        self.device = _device(device)
         self._taps = _taps(kernel, self.power, self.device)
         self.plan = torch.empty(nb, dtype=torch.uint8, device=self.device)
         stream = torch.cuda.current_stream(self.device).cuda_stream

@@ -161,3 +161,18 @@ def test_range_compression_plan_and_apply_check_arguments_first():
     ]
     for got, want in cases:
         assert got == want
+
+
+@pytest.mark.parametrize("args,kw", [
+    ((np.ones(3), 3, 100), {}),                       # center past the taps
+    ((np.ones(3), 1, 0), {}),                         # no samples
+    ((np.ones(1201), 600, 8000), {}),                 # above the FFT limit
+    ((np.ones(3), 1, 100), {"precision": "fp16"}),    # unknown precision
+])
+def test_range_compressor_checks_arguments_before_the_device(args, kw):
+    """Bad pulse-plan arguments raise ValueError before any device
+    resolution, allocation or copy (on this host a device step would raise
+    a CUDA error instead)."""
+    from radar_sounder_simulator_gb300.waveform import RangeCompressor
+    with pytest.raises(ValueError):
+        RangeCompressor(*args, **kw)
